@@ -1,0 +1,377 @@
+"""Benchmark of the prescaler hot path on one GB300 (or N replicas).
+
+Workload (one *step*): the 1080p -> 2160p batch of the reference's second
+benchmark configuration -- 8 synthetic 1920x1080 luma planes stored FP16,
+each upscaled 2x by ravu-lite-ar-r4 (anti-ringing 0.8) and by two-pass
+ravu-r3, i.e. 16 output frames of 3840x2160 per step.  Planes come from the
+seeded generator (seed 2000 + frame); LUTs are the ones parsed from the
+``.hook`` files when the model cache is present, otherwise seeded synthetic
+LUTs of the same shapes (``config.weights`` says which).
+
+Reported (one JSON line on rank 0):
+
+* ``value``: output Mpix/s of the chosen form (FP16 planes, FP32 math), all
+  ranks together, inputs resident in HBM; ``fp32_value``: the plain FP32
+  form (FP32 planes) on the same workload.
+* ``e2e``: the same metric through ``HookModel.upscale`` with the frames
+  copied host->device (pinned) and the upscaled frames copied back every step.
+* ``roofline``: the dominant kernel (ravu-lite-ar-r4, FP16 planes) against
+  the FP32 pipe; ``hbm`` against measured copy bandwidth.
+* ``cpu_baseline``: the FP64 NumPy oracle on a bounded sample of the same
+  workload, on the host's cores.
+* ``headline``: chosen vs plain FP32 Mpix/s for ravu-lite-ar-r3 and
+  nnedi3-nns128-win8x6 on 1920x1080 -> 3840x2160.
+
+``--impl reference`` times the reference arm: the CPU restatement of the
+shader arithmetic (the reference's shaders need an OpenGL/Vulkan host that
+this machine does not have), on all host cores, same metric and workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+import __graft_entry__ as _entry  # noqa: E402
+
+H, W, NFRAMES = 1080, 1920, 8
+MODELS = ("ravu-lite-ar-r4", "ravu-r3")
+SEED0 = 2000
+# algorithmic FP32 flops per INPUT pixel (structure tensor 13/point, eigen+key
+# 35, filter 8/tap, anti-ringing 48/AR tap + 32; lattice ravu: 3 keyed passes)
+FLOPS_PER_IN_PX = {"ravu-lite-ar-r4": 13 * 25 + 35 + 8 * 49 + 48 * 13 + 32,
+                   "ravu-lite-ar-r3": 13 * 9 + 35 + 8 * 25 + 48 * 13 + 32,
+                   "ravu-r3": 3 * (13 * 16 + 35 + 1.5 * 36 + 2)}
+
+
+def _pkg():
+    return _entry._package()
+
+
+# ------------------------------------------------------------------ CPU ---
+
+def _cpu_strip(args):
+    """Oracle on rows [y0, y1) of one frame (with the window halo)."""
+    name, y0, y1, seed = args
+    sys.path.insert(0, REPO)
+    pkg = _pkg()
+    from mpv_prescalers_gb300 import synth
+    import oracle
+    hm, _ = synth.model_for(name)
+    x = synth.luma_plane(H, W, seed)
+    pad = 8
+    a, b = max(0, y0 - pad), min(H, y1 + pad)
+    t = time.perf_counter()
+    y, _ = oracle.keyed_upscale(hm.model, x[a:b])
+    dt = time.perf_counter() - t
+    return (y1 - y0) * W * 4, dt
+
+
+def cpu_baseline(rows_per_model: int, workers: int):
+    """Oracle Mpix/s on a bounded sample: `rows_per_model` input rows of frame
+    0 per model, split in strips over `workers` spawned processes."""
+    ctx = mp.get_context("spawn")
+    tasks = []
+    strip = max(8, rows_per_model // workers)
+    for name in MODELS:
+        for y0 in range(0, rows_per_model, strip):
+            tasks.append((name, y0, min(rows_per_model, y0 + strip), SEED0))
+    with ctx.Pool(workers) as pool:
+        pool.map(_cpu_strip, [(MODELS[0], 0, 8, SEED0)] * workers)  # warm the workers
+        t = time.perf_counter()
+        res = pool.map(_cpu_strip, tasks)
+        wall = time.perf_counter() - t
+    px = sum(r[0] for r in res)
+    return {"value": px / wall / 1e6, "unit": "Mpix/s", "cores": workers, "kind": "port",
+            "sample": f"{rows_per_model} of {H} input rows of one 1920x1080 frame per model "
+                      f"({', '.join(MODELS)}), FP64 NumPy oracle, {len(tasks)} strips on {workers} processes",
+            "seconds": wall}
+
+
+# ---------------------------------------------------------------- clocks ---
+
+class Clocks:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            f = [v.strip() for v in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------- GPU ---
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+    pkg = _pkg()
+    from mpv_prescalers_gb300 import synth
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    models, sources = {}, {}
+    for n in MODELS + ("ravu-lite-ar-r3", "nnedi3-nns128-win8x6"):
+        models[n], sources[n] = synth.model_for(n)
+    frames = np.stack([synth.luma_plane(H, W, SEED0 + f) for f in range(NFRAMES)])
+    x16 = torch.from_numpy(frames).to(dev, torch.float16)
+    x32 = torch.from_numpy(frames).to(dev, torch.float32)
+    outs16 = {n: torch.empty((NFRAMES, 2 * H, 2 * W), dtype=torch.float16, device=dev) for n in MODELS}
+    outs32 = {n: torch.empty((NFRAMES, 2 * H, 2 * W), dtype=torch.float32, device=dev) for n in MODELS}
+    stream = torch.cuda.current_stream(dev)
+    launches_per_step = NFRAMES * (1 + 2)  # lite: 1 kernel/frame, lattice: 2
+
+    def step(xs, outs, ev=None):
+        for n in MODELS:
+            hm = models[n]
+            for f in range(NFRAMES):
+                if ev is not None and n == MODELS[0]:
+                    ev.append((torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)))
+                    ev[-1][0].record(stream)
+                hm.run_raw([xs[f]], [outs[n][f]], out_size=(2 * W, 2 * H), stream=stream)
+                if ev is not None and n == MODELS[0]:
+                    ev[-1][1].record(stream)
+
+    def timed(xs, outs, steps, warmup, kernel_events=None):
+        for _ in range(warmup):
+            step(xs, outs)
+        torch.cuda.synchronize()
+        barrier()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(steps):
+            step(xs, outs, kernel_events)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ms = t0.elapsed_time(t1)
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    out_px_step = len(MODELS) * NFRAMES * (2 * W) * (2 * H)
+    kev = []
+    with Clocks(local) as clk:
+        ms16 = timed(x16, outs16, args.steps, args.warmup, kev)
+    ms32 = timed(x32, outs32, args.steps, args.warmup)
+    value = world * out_px_step * args.steps / (ms16 / 1e3) / 1e6
+    fp32_value = world * out_px_step * args.steps / (ms32 / 1e3) / 1e6
+    kern_ms = statistics.mean(a.elapsed_time(b) for a, b in kev)
+
+    # ---- end to end: pinned host frames in, upscaled frames back, per step
+    host_in = torch.from_numpy(frames).to(torch.float16).pin_memory()
+    host_out = {n: torch.empty((NFRAMES, 2 * H, 2 * W), dtype=torch.float16).pin_memory() for n in MODELS}
+
+    def e2e_step():
+        xd = host_in.to(dev, non_blocking=True)
+        for n in MODELS:
+            y = models[n].upscale(xd.unsqueeze(1))  # public API, [N][C][H][W] frames in, new tensor out
+            host_out[n].copy_(y.squeeze(1), non_blocking=True)
+
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_ms = e0.elapsed_time(e1)
+    e2e_value = world * out_px_step * args.steps / (e2e_ms / 1e3) / 1e6
+
+    # ---- headline pairs at 1080p -> 2160p (single frame, chosen vs FP32)
+    headline = {}
+    for n in ("ravu-lite-ar-r3", "nnedi3-nns128-win8x6"):
+        hm = models[n]
+        res = {}
+        for prec, dt in (("fast", torch.float16), ("fp32", torch.float32)):
+            xi = x32[0].to(dt)
+            yo = torch.empty((2 * H, 2 * W), dtype=dt, device=dev)
+            scratch = torch.empty(2 * H * W * xi.element_size(), dtype=torch.uint8, device=dev)
+            for _ in range(3):
+                hm.run_raw([xi], [yo], out_size=(2 * W, 2 * H), precision=prec, scratch=scratch)
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            reps = 10
+            a.record(stream)
+            for _ in range(reps):
+                hm.run_raw([xi], [yo], out_size=(2 * W, 2 * H), precision=prec, scratch=scratch)
+            b.record(stream)
+            torch.cuda.synchronize()
+            res[prec] = 4 * H * W * reps / (a.elapsed_time(b) / 1e3) / 1e6
+        headline[n] = {"chosen_mpix_s": res["fast"], "fp32_mpix_s": res["fp32"],
+                       "ratio": res["fast"] / res["fp32"], "chosen": "FP16 planes" + (
+                           ", FP16 tensor-core neurons" if n.startswith("nnedi3") else ", FP32 math")}
+
+    props = torch.cuda.get_device_properties(dev)
+    clocks = clk.summary()
+    sm_mhz = clocks["sm_mhz"] or 0.0
+    fl = FLOPS_PER_IN_PX[MODELS[0]] * H * W
+    achieved_tf = fl / (kern_ms / 1e3) / 1e12
+    max_mhz = clocks.get("sm_max_mhz") or 2070.0
+    peak_tf = props.multi_processor_count * 256 * max_mhz * 1e6 / 1e12
+    algo_bytes = H * W * 2 + 4 * H * W * 2  # FP16 plane in + 2x2 FP16 out
+    peaks = {}
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    line = {
+        "metric": "Out Mpix/s 1080p->2160p (ravu-lite-ar-r4 + two-pass ravu-r3, 8 frames each)",
+        "value": value, "unit": "Mpix/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms16 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp16 planes, fp32 math", "data": "synthetic (seeded sinusoids+polygons+noise)",
+        "config": {"workload": "8x 1920x1080 FP16 luma -> 3840x2160 through ravu-lite-ar-r4 and ravu-r3",
+                   "frames_per_model": NFRAMES, "weights": {n: sources[n] for n in MODELS},
+                   "l2": "per-model working set 166 MB (33 MB in + 133 MB out) > 129 MB L2",
+                   "parallelism": f"replicas x{world}"},
+        "fp32_value": fp32_value, "chosen_vs_fp32": value / fp32_value,
+        "e2e": {"value": e2e_value, "unit": "Mpix/s",
+                "h2d_bytes_per_step": int(host_in.numel() * host_in.element_size()),
+                "d2h_bytes_per_step": int(sum(t.numel() * t.element_size() for t in host_out.values()))},
+        "roofline": {"bound": "fp32", "kernel": "lite_kernel<4,AR,half> (ravu-lite-ar-r4)",
+                     "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s", "frac": achieved_tf / peak_tf,
+                     "peak_source": f"{props.multi_processor_count} SMs x 128 FFMA/clk x 2 x {max_mhz:.0f} MHz "
+                                    "(FP32 pipe; not in MEASURED_PEAKS.json)",
+                     "flops_per_launch": fl, "launch_ms": kern_ms,
+                     "hbm": {"achieved": algo_bytes / (kern_ms / 1e3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                             "frac": algo_bytes / (kern_ms / 1e3) / 1e9 / hbm_peak,
+                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
+                     "traffic": None},
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": clocks,
+        "headline": headline,
+        "device": props.name,
+    }
+    if world > 1:
+        dist.destroy_process_group()
+    return line if rank == 0 else None
+
+
+# ------------------------------------------------------------- reference ---
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return None
+    workers = len(os.sched_getaffinity(0))
+    rows = args.ref_rows
+    for _ in range(max(0, min(args.warmup, 1))):
+        cpu_baseline(16, workers)
+    vals = []
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(rows, workers))
+    v = statistics.mean(r["value"] for r in vals)
+    cb = dict(vals[-1])
+    cb["value"] = v
+    return {"impl": "reference", "metric": "Out Mpix/s 1080p->2160p (ravu-lite-ar-r4 + two-pass ravu-r3, 8 frames each)",
+            "value": v, "unit": "Mpix/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": statistics.mean(r["seconds"] for r in vals) * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded sinusoids+polygons+noise)",
+            "config": {"workload": "8x 1920x1080 FP16 luma -> 3840x2160 through ravu-lite-ar-r4 and ravu-r3",
+                       "sample": cb["sample"]},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "reference shaders need mpv + OpenGL/Vulkan (unavailable on this box); the reference arm is "
+                    "the CPU restatement of their arithmetic (FP64 NumPy), all host cores"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-rows", type=int, default=96, help="input rows per model in the CPU sample")
+    ap.add_argument("--ref-rows", type=int, default=64)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        args.warmup = 3
+    if args.impl == "reference":
+        line = run_reference(args)
+        if line:
+            print(json.dumps(line))
+        return
+    rank = int(os.environ.get("RANK", "0"))
+    cb = None
+    if rank == 0 and not args.no_cpu:  # the CPU pool starts before any GPU call
+        cb = cpu_baseline(args.cpu_rows, len(os.sched_getaffinity(0)))
+    line = run_gpu(args)
+    if line is not None:
+        line["cpu_baseline"] = cb
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,156 @@
+/*
+ * prescale.h -- C ABI of the GB300-native RAVU / NNEDI3 prescaler library
+ * (libprescale.so).
+ *
+ * The reference has no library boundary of its own: its "interface" is the
+ * mpv user-shader hook protocol.  A host (mpv, libplacebo) parses a .hook
+ * file, uploads the //!TEXTURE blocks once, and for every frame binds the
+ * hooked plane and dispatches each pass.  The entry points below are what
+ * such a host binds instead of the shader passes:
+ *
+ *   pz_model_create   replaces the one-time //!TEXTURE upload and the
+ *                     per-file constants (e.g. ravu-lite-r3.hook:132-136
+ *                     LUT block; nnedi3-nns16-win8x4.hook:31-49 inline
+ *                     weights; ravu-lite-ar-r3.hook:181 AR strength).
+ *   pz_run            replaces one full hook chain on one frame:
+ *                     ravu-lite(-ar): ravu-lite-r3.hook:15-131 (2 passes),
+ *                       compute/ravu-lite-ar-r3.hook:15-171 (1 pass);
+ *                     ravu: ravu-r3.hook:15-437 (4 passes),
+ *                       compute/ravu-r3.hook:15-430 (2 passes);
+ *                     ravu-zoom(-ar): ravu-zoom-r2.hook:15-139,
+ *                       compute/ravu-zoom-ar-r2-rgb.hook:15-238;
+ *                     ravu-3x: compute/ravu-3x-r2.hook:15-115;
+ *                     nnedi3: nnedi3-nns16-win8x4.hook:15-210 (4 passes),
+ *                       compute/nnedi3-nns128-win8x6.hook:15-448 (2 passes).
+ *   pz_batch_run      replaces many such dispatches (mixed files, frames of
+ *                     uneven size) issued back to back by the host, as one
+ *                     persistent launch.
+ *
+ * Conventions: all buffers are caller-owned DEVICE memory; every call is
+ * asynchronous on the given CUDA stream; return codes are 0 or a negative
+ * errno value, with a message for the calling thread in pz_last_error().
+ * No C++ exception crosses this boundary.  A model is immutable after
+ * creation and may be used from several streams at once.
+ */
+#ifndef PRESCALE_H
+#define PRESCALE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PZ_ABI_VERSION 1
+
+#define PZ_OK 0
+#define PZ_EINVAL (-22)
+#define PZ_ENOMEM (-12)
+#define PZ_EIO (-5)         /* CUDA launch or runtime error */
+#define PZ_ENOTSUP (-95)
+#define PZ_ETIMEDOUT (-110) /* a bounded device-side wait ran out */
+
+typedef enum {
+  PZ_RAVU_LITE = 1, /* ravu-lite, ravu-lite-ar            */
+  PZ_RAVU = 2,      /* ravu (lattice: int11, int10, int01) */
+  PZ_RAVU_ZOOM = 3, /* ravu-zoom, ravu-zoom-ar             */
+  PZ_RAVU_3X = 4,   /* ravu-3x                             */
+  PZ_NNEDI3 = 5
+} pz_family;
+
+typedef enum { PZ_LUMA = 0, PZ_YUV = 1, PZ_RGB = 2 } pz_channels;
+typedef enum { PZ_F32 = 0, PZ_F16 = 1 } pz_dtype;
+
+typedef enum {
+  PZ_PREC_FP32 = 0,  /* plain FP32 arithmetic everywhere                    */
+  PZ_PREC_FAST = 1   /* FP16 tensor-core NNEDI3 neurons; RAVU unchanged     */
+} pz_precision;
+
+/* Everything a .hook file contributes; host arrays are copied. */
+typedef struct {
+  int family;              /* pz_family                                      */
+  int radius;              /* RAVU radius (2, 3, 4)                          */
+  int channels;            /* pz_channels                                    */
+  float ar_strength;       /* anti-ringing mix strength, 0 = none            */
+  /* RAVU LUT: float32 [lut_rows][lut_cols][4] exactly as in //!TEXTURE      */
+  const float* lut;
+  int lut_rows, lut_cols;
+  const float* lut_ar;     /* ravu-zoom-ar second LUT (same shape) or NULL   */
+  /* key quantisation */
+  const double* grad_weights; /* Gaussian weights of the gradient points     */
+  int n_grad;
+  int strength_log2;       /* 0: thresholds, 1: floor(log2(l*scale+eps))    */
+  float strength_thr[3];
+  int n_strength_thr;      /* 2 or 3 when strength_log2 == 0                 */
+  float strength_scale;    /* e.g. 2000                                      */
+  int strength_max;        /* e.g. 8                                         */
+  float coherence_thr[2];  /* 0.25, 0.5                                      */
+  /* NNEDI3 */
+  int nns, win_w, win_h;
+  const float* weights_a;  /* [win_w*win_h][nns], canonical tap order        */
+  const float* weights_b;
+  const float* bias_a;     /* [nns] */
+  const float* bias_b;
+} pz_model_desc;
+
+typedef struct pz_model pz_model;
+
+/* One image plane in device memory (pitch in elements). */
+typedef struct {
+  void* data;
+  int width, height;
+  int pitch;
+  int dtype;               /* pz_dtype */
+} pz_plane;
+
+typedef struct {
+  int precision;           /* pz_precision                                   */
+  int out_width;           /* ravu-zoom target size; ignored otherwise       */
+  int out_height;
+  int nnedi3_axes;         /* bit 0: double rows (y), bit 1: columns (x);
+                              0 means both                                   */
+  int32_t* keys;           /* optional device buffer receiving the raw LUT
+                              key of every key evaluation (parity tests)     */
+  void* scratch;           /* optional caller scratch for multi-pass chains  */
+  size_t scratch_bytes;
+} pz_opts;
+
+int pz_version(void);
+const char* pz_last_error(void);
+
+int pz_model_create(const pz_model_desc* desc, pz_model** out);
+void pz_model_destroy(pz_model* model);
+
+/* Device scratch bytes pz_run needs for this model/input (0 if none). */
+size_t pz_scratch_bytes(const pz_model* model, const pz_plane* in, const pz_opts* opts);
+
+/* Run the full hook chain of `model` on one frame.  n_in/n_out planes are
+ * 1 (luma) or 3 (yuv/rgb, planar).  Output sizes: 2x (lite, ravu, nnedi3),
+ * 3x (3x), or opts->out_width x out_height (zoom).  When opts->scratch is
+ * NULL and scratch is needed, it is allocated stream-ordered and freed. */
+int pz_run(const pz_model* model, const pz_plane* in, int n_in, pz_plane* out, int n_out,
+           const pz_opts* opts, void* cuda_stream);
+
+/* ---- batched persistent execution ------------------------------------- */
+
+typedef struct {
+  const pz_model* model;
+  pz_plane in[3];
+  pz_plane out[3];
+  int n_planes;
+  pz_opts opts;
+} pz_job;
+
+/* Run many jobs (any mix of RAVU models, any frame sizes) in one persistent
+ * launch over a device work queue of tiles.  Jobs whose chain needs more
+ * than one dependent pass (ravu lattice, nnedi3) are run as phases.
+ * `work` is caller device memory of at least pz_batch_work_bytes(). */
+size_t pz_batch_work_bytes(const pz_job* jobs, int n_jobs);
+int pz_batch_run(const pz_job* jobs, int n_jobs, void* work, size_t work_bytes,
+                 void* cuda_stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PRESCALE_H */

@@ -1,0 +1,375 @@
+// C ABI of libprescale.so (declared in include/prescale.h): model upload,
+// argument checking, dispatch to the kernels, thread-local error messages.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/prescale.h"
+#include "kernels.h"
+
+struct pz_model {
+  int family = 0, radius = 0, channels = 0;
+  float ar = 0.0f;
+  float4* d_lut = nullptr;
+  float4* d_lut_ar = nullptr;
+  int lut_rows = 0, lut_cols = 0;
+  pz::KeyParams kp{};
+  int nns = 0, win_w = 0, win_h = 0;
+  float* d_wts = nullptr;   // [nns][2][T]
+  float* d_cs = nullptr;    // [nns][2]
+  float* d_bias = nullptr;  // [nns][2]
+  __half* d_wts_h = nullptr;
+  int device = 0;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(PZ_EIO, "%s: %s", what, cudaGetErrorString(e));
+}
+
+template <typename T>
+int upload(T** dst, const void* src, size_t bytes) {
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(dst), bytes);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+  e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy");
+  return PZ_OK;
+}
+
+std::mutex g_err_mu;
+std::vector<int*> g_err_words;  // per device
+
+size_t dtype_size(int dt) { return dt == PZ_F32 ? 4 : 2; }
+
+// `pairs`: the plane is written with 2-wide vector stores, so its base and
+// pitch must keep every even column 2-element aligned.
+int check_plane(const pz_plane& p, const char* what, int idx, bool pairs) {
+  if (!p.data) return fail(PZ_EINVAL, "%s[%d]: null data", what, idx);
+  if (p.width <= 0 || p.height <= 0) return fail(PZ_EINVAL, "%s[%d]: bad size %dx%d", what, idx, p.width, p.height);
+  if (p.pitch < p.width) return fail(PZ_EINVAL, "%s[%d]: pitch %d < width %d", what, idx, p.pitch, p.width);
+  if (p.dtype != PZ_F32 && p.dtype != PZ_F16) return fail(PZ_EINVAL, "%s[%d]: unknown dtype %d", what, idx, p.dtype);
+  const size_t es = dtype_size(p.dtype);
+  if ((reinterpret_cast<uintptr_t>(p.data) % es) != 0)
+    return fail(PZ_EINVAL, "%s[%d]: data not aligned to its element size", what, idx);
+  if (pairs && ((reinterpret_cast<uintptr_t>(p.data) % (2 * es)) != 0 || (p.pitch % 2) != 0))
+    return fail(PZ_EINVAL, "%s[%d]: this output is written in pixel pairs; base and pitch must be 2-element aligned",
+                what, idx);
+  return PZ_OK;
+}
+
+}  // namespace
+
+namespace pz {
+int* device_error_word() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  if ((int)g_err_words.size() <= dev) g_err_words.resize(dev + 1, nullptr);
+  if (!g_err_words[dev]) {
+    int* w = nullptr;
+    if (cudaMalloc(&w, sizeof(int)) != cudaSuccess) return nullptr;
+    if (cudaMemset(w, 0, sizeof(int)) != cudaSuccess) return nullptr;
+    g_err_words[dev] = w;
+  }
+  return g_err_words[dev];
+}
+}  // namespace pz
+
+extern "C" {
+
+int pz_version(void) { return PZ_ABI_VERSION; }
+
+const char* pz_last_error(void) { return g_err.c_str(); }
+
+int pz_model_create(const pz_model_desc* d, pz_model** out) {
+  if (!d || !out) return fail(PZ_EINVAL, "null argument");
+  *out = nullptr;
+  pz_model* m = new (std::nothrow) pz_model();
+  if (!m) return fail(PZ_ENOMEM, "host allocation failed");
+  cudaGetDevice(&m->device);
+  m->family = d->family;
+  m->radius = d->radius;
+  m->channels = d->channels;
+  m->ar = d->ar_strength;
+  int rc = PZ_OK;
+  if (d->family == PZ_NNEDI3) {
+    if (d->nns <= 0 || d->nns % 8 || d->win_w != 8 || (d->win_h != 4 && d->win_h != 6) || !d->weights_a ||
+        !d->weights_b || !d->bias_a || !d->bias_b) {
+      delete m;
+      return fail(PZ_EINVAL, "bad NNEDI3 description (nns %d, window %dx%d)", d->nns, d->win_w, d->win_h);
+    }
+    m->nns = d->nns;
+    m->win_w = d->win_w;
+    m->win_h = d->win_h;
+    const int T = d->win_w * d->win_h, n = d->nns;
+    std::vector<float> w((size_t)n * 2 * T), cs((size_t)n * 2), bias((size_t)n * 2);
+    std::vector<__half> wh((size_t)n * 2 * T);
+    for (int k = 0; k < n; k++) {
+      double sa = 0, sb = 0;
+      for (int t = 0; t < T; t++) {
+        float a = d->weights_a[(size_t)t * n + k], b = d->weights_b[(size_t)t * n + k];
+        w[((size_t)k * 2 + 0) * T + t] = a;
+        w[((size_t)k * 2 + 1) * T + t] = b;
+        sa += a;
+        sb += b;
+      }
+      cs[2 * k] = (float)sa;
+      cs[2 * k + 1] = (float)sb;
+      bias[2 * k] = d->bias_a[k];
+      bias[2 * k + 1] = d->bias_b[k];
+    }
+    for (size_t i = 0; i < w.size(); i++) wh[i] = __float2half_rn(w[i]);
+    if ((rc = upload(&m->d_wts, w.data(), w.size() * 4)) || (rc = upload(&m->d_cs, cs.data(), cs.size() * 4)) ||
+        (rc = upload(&m->d_bias, bias.data(), bias.size() * 4)) ||
+        (rc = upload(&m->d_wts_h, wh.data(), wh.size() * 2))) {
+      pz_model_destroy(m);
+      return rc;
+    }
+    *out = m;
+    return PZ_OK;
+  }
+  if (d->family < PZ_RAVU_LITE || d->family > PZ_RAVU_3X) {
+    delete m;
+    return fail(PZ_EINVAL, "unknown family %d", d->family);
+  }
+  const int maxr = d->family == PZ_RAVU_ZOOM ? 3 : 4;
+  if (d->radius < 2 || d->radius > maxr) {
+    delete m;
+    return fail(PZ_ENOTSUP, "radius %d not supported for family %d", d->radius, d->family);
+  }
+  if (d->channels < PZ_LUMA || d->channels > PZ_RGB || (d->family == PZ_RAVU_LITE && d->channels != PZ_LUMA)) {
+    delete m;
+    return fail(PZ_EINVAL, "bad channels %d for family %d", d->channels, d->family);
+  }
+  if (!d->lut || d->lut_rows <= 0 || d->lut_cols <= 0 || !d->grad_weights || d->n_grad <= 0 || d->n_grad > 36) {
+    delete m;
+    return fail(PZ_EINVAL, "bad LUT / gradient description");
+  }
+  const int n = d->family == PZ_RAVU_LITE || d->family == PZ_RAVU_3X ? 2 * d->radius - 1 : 2 * d->radius;
+  const int pts = n <= 4 ? n * n : (n - 2) * (n - 2);
+  if (d->n_grad != pts) {
+    delete m;
+    return fail(PZ_EINVAL, "%d gradient weights, window needs %d", d->n_grad, pts);
+  }
+  pz::KeyParams& kp = m->kp;
+  for (int i = 0; i < d->n_grad; i++) kp.gw[i] = (float)d->grad_weights[i];
+  kp.log2_mode = d->strength_log2;
+  if (kp.log2_mode) {
+    kp.log2_scale = d->strength_scale;
+    kp.log2_max = (float)d->strength_max;
+    kp.n_strength = d->strength_max + 1;
+  } else {
+    if (d->n_strength_thr != 2 && d->n_strength_thr != 3) {
+      delete m;
+      return fail(PZ_EINVAL, "need 2 or 3 strength thresholds");
+    }
+    kp.n_thr = d->n_strength_thr;
+    for (int i = 0; i < kp.n_thr; i++) kp.thr[i] = d->strength_thr[i];
+    kp.n_strength = kp.n_thr + 1;
+  }
+  kp.coh0 = d->coherence_thr[0];
+  kp.coh1 = d->coherence_thr[1];
+  kp.rows = 24 * kp.n_strength * 3;
+  const int want_rows = d->family == PZ_RAVU_ZOOM ? kp.rows * 9 : kp.rows;
+  if (d->lut_rows != want_rows) {
+    delete m;
+    return fail(PZ_EINVAL, "LUT has %d rows, key layout needs %d", d->lut_rows, want_rows);
+  }
+  const int S = n * n;
+  int need_cols = 0;
+  switch (d->family) {
+    case PZ_RAVU_LITE: need_cols = (S + 1) / 2; break;
+    case PZ_RAVU: need_cols = (S / 2 + 3) / 4; break;
+    case PZ_RAVU_3X: need_cols = 2 * ((S + 1) / 2); break;
+    case PZ_RAVU_ZOOM: need_cols = 9 * ((S / 2 + 3) / 4); break;
+  }
+  if (d->lut_cols != need_cols) {
+    delete m;
+    return fail(PZ_EINVAL, "LUT has %d columns, radius %d needs %d", d->lut_cols, d->radius, need_cols);
+  }
+  if (d->family == PZ_RAVU_ZOOM && (d->ar_strength != 0.0f) != (d->lut_ar != nullptr)) {
+    delete m;
+    return fail(PZ_EINVAL, "ravu-zoom anti-ringing needs the _ar LUT and a strength");
+  }
+  m->lut_rows = d->lut_rows;
+  m->lut_cols = d->lut_cols;
+  const size_t bytes = (size_t)d->lut_rows * d->lut_cols * 16;
+  if ((rc = upload(&m->d_lut, d->lut, bytes))) {
+    pz_model_destroy(m);
+    return rc;
+  }
+  if (d->lut_ar && (rc = upload(&m->d_lut_ar, d->lut_ar, bytes))) {
+    pz_model_destroy(m);
+    return rc;
+  }
+  *out = m;
+  return PZ_OK;
+}
+
+void pz_model_destroy(pz_model* m) {
+  if (!m) return;
+  cudaFree(m->d_lut);
+  cudaFree(m->d_lut_ar);
+  cudaFree(m->d_wts);
+  cudaFree(m->d_cs);
+  cudaFree(m->d_bias);
+  cudaFree(m->d_wts_h);
+  delete m;
+}
+
+static int nn_axes(const pz_opts* o) {
+  int ax = o ? o->nnedi3_axes : 0;
+  return ax == 0 ? 3 : ax;
+}
+
+size_t pz_scratch_bytes(const pz_model* m, const pz_plane* in, const pz_opts* o) {
+  if (!m || !in || m->family != PZ_NNEDI3 || nn_axes(o) != 3) return 0;
+  return (size_t)2 * in->height * in->width * dtype_size(in->dtype);
+}
+
+int pz_run(const pz_model* m, const pz_plane* in, int n_in, pz_plane* out, int n_out, const pz_opts* o,
+           void* stream) {
+  if (!m || !in || !out) return fail(PZ_EINVAL, "null argument");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int C = m->channels == PZ_LUMA ? 1 : 3;
+  if (n_in != C || n_out != C) return fail(PZ_EINVAL, "model needs %d planes, got %d in / %d out", C, n_in, n_out);
+  int rc;
+  const bool pairs = m->family == PZ_RAVU_LITE || (m->family == PZ_NNEDI3 && (nn_axes(o) & 2));
+  for (int c = 0; c < C; c++) {
+    if ((rc = check_plane(in[c], "in", c, false)) || (rc = check_plane(out[c], "out", c, pairs))) return rc;
+    if (in[c].width != in[0].width || in[c].height != in[0].height)
+      return fail(PZ_EINVAL, "input planes differ in size");
+    if (in[c].dtype != in[0].dtype || out[c].dtype != in[0].dtype)
+      return fail(PZ_EINVAL, "all planes must share one dtype");
+    if (out[c].width != out[0].width || out[c].height != out[0].height)
+      return fail(PZ_EINVAL, "output planes differ in size");
+  }
+  const int W = in[0].width, H = in[0].height, dt = in[0].dtype;
+  int OW = 2 * W, OH = 2 * H;
+  if (m->family == PZ_RAVU_3X) {
+    OW = 3 * W;
+    OH = 3 * H;
+  } else if (m->family == PZ_RAVU_ZOOM) {
+    if (!o) return fail(PZ_EINVAL, "ravu-zoom needs opts->out_width/out_height");
+    OW = o->out_width;
+    OH = o->out_height;
+    if (OW <= W || OH <= H)
+      return fail(PZ_EINVAL, "ravu-zoom upscales only (//!WHEN in < out): %dx%d -> %dx%d", W, H, OW, OH);
+  } else if (m->family == PZ_NNEDI3) {
+    const int ax = nn_axes(o);
+    OW = (ax & 2) ? 2 * W : W;
+    OH = (ax & 1) ? 2 * H : H;
+  }
+  if (out[0].width != OW || out[0].height != OH)
+    return fail(PZ_EINVAL, "output must be %dx%d, got %dx%d", OW, OH, out[0].width, out[0].height);
+
+  if (m->family == PZ_NNEDI3) {
+    const int ax = nn_axes(o);
+    const bool fast = o && o->precision == PZ_PREC_FAST && pz::nnedi3_tc_supported(m->nns, m->win_h);
+    pz::NnArgs a{};
+    a.nns = m->nns;
+    a.win_h = m->win_h;
+    a.wts = m->d_wts;
+    a.cs = m->d_cs;
+    a.bias = m->d_bias;
+    a.wts_h = m->d_wts_h;
+    a.err = pz::device_error_word();
+    void* tmp = nullptr;
+    bool own_tmp = false;
+    if (ax == 3) {
+      const size_t need = (size_t)2 * H * W * dtype_size(dt);
+      if (o && o->scratch) {
+        if (o->scratch_bytes < need) return fail(PZ_EINVAL, "scratch %zu bytes < %zu needed", o->scratch_bytes, need);
+        tmp = o->scratch;
+      } else {
+        cudaError_t e = cudaMallocAsync(&tmp, need, s);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync(scratch)");
+        own_tmp = true;
+      }
+    }
+    auto pass = [&](bool xpass, const void* src, int sw, int sh, int spitch, void* dst, int dpitch) {
+      a.in = src;
+      a.in_pitch = spitch;
+      a.out = dst;
+      a.out_pitch = dpitch;
+      a.W = sw;
+      a.H = sh;
+      return fast ? pz::launch_nnedi3_tc(a, xpass, dt, s) : pz::launch_nnedi3_simt(a, xpass, dt, s);
+    };
+    rc = 0;
+    if (ax == 3) {
+      rc = pass(false, in[0].data, W, H, in[0].pitch, tmp, W);
+      if (!rc) rc = pass(true, tmp, W, 2 * H, W, out[0].data, out[0].pitch);
+    } else if (ax == 1) {
+      rc = pass(false, in[0].data, W, H, in[0].pitch, out[0].data, out[0].pitch);
+    } else {
+      rc = pass(true, in[0].data, W, H, in[0].pitch, out[0].data, out[0].pitch);
+    }
+    if (own_tmp) cudaFreeAsync(tmp, s);
+    if (rc) return fail(rc, "NNEDI3 launch configuration not supported");
+  } else {
+    pz::RavuArgs a{};
+    for (int c = 0; c < C; c++) {
+      a.in[c] = in[c].data;
+      a.in_pitch[c] = in[c].pitch;
+      a.out[c] = out[c].data;
+      a.out_pitch[c] = out[c].pitch;
+    }
+    a.W = W;
+    a.H = H;
+    a.OW = OW;
+    a.OH = OH;
+    a.lut = m->d_lut;
+    a.lut_ar = m->d_lut_ar;
+    a.lut_rows = m->lut_rows;
+    a.lut_cols = m->lut_cols;
+    a.ar = m->ar;
+    a.keys = o ? o->keys : nullptr;
+    a.kp = m->kp;
+    switch (m->family) {
+      case PZ_RAVU_LITE: rc = pz::launch_lite(a, m->radius, m->ar != 0.0f, dt, s); break;
+      case PZ_RAVU_3X: rc = pz::launch_3x(a, m->radius, m->channels, dt, s); break;
+      case PZ_RAVU: rc = pz::launch_lattice(a, m->radius, m->channels, dt, s); break;
+      case PZ_RAVU_ZOOM: rc = pz::launch_zoom(a, m->radius, m->channels, m->ar != 0.0f, dt, s); break;
+      default: rc = PZ_EINVAL;
+    }
+    if (rc) return fail(rc, "no kernel for family %d radius %d", m->family, m->radius);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+  return PZ_OK;
+}
+
+size_t pz_batch_work_bytes(const pz_job* jobs, int n_jobs) {
+  (void)jobs;
+  (void)n_jobs;
+  return 0;
+}
+
+int pz_batch_run(const pz_job* jobs, int n_jobs, void* work, size_t work_bytes, void* stream) {
+  (void)jobs;
+  (void)n_jobs;
+  (void)work;
+  (void)work_bytes;
+  (void)stream;
+  return fail(PZ_ENOTSUP, "batched execution not built yet");
+}
+
+}  // extern "C"

@@ -1,0 +1,146 @@
+// Shared device code for the prescaler kernels (sm_103a).
+//
+// The arithmetic mirrors the reference shaders expression by expression
+// where that matters for the key (the quantised LUT row):
+//   structure tensor   ravu-lite-r3.hook:48-76, ravu-r3.hook:58-107
+//   eigen/key          ravu-lite-r3.hook:77-88, ravu-r3.hook:108-125
+// All key math is FP32, IEEE division and square root (no fast-math).
+#pragma once
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pz {
+
+constexpr float kFltEps = 1.192092896e-7f;   // the shaders' epsilon literal
+constexpr float kPi = 3.141592653589793f;    // the shaders' pi literal
+
+// Key quantisation constants of one model (kernel parameter).
+struct KeyParams {
+  float gw[36];      // Gaussian weights of the gradient points (geometry order)
+  float thr[3];      // strength thresholds (lite, zoom: 3; 3x: 2)
+  int n_thr;
+  int log2_mode;     // ravu: strength = clamp(floor(log2(l*scale+eps)), 0, max)
+  float log2_scale;
+  float log2_max;
+  float coh0, coh1;  // coherence thresholds
+  int n_strength;    // strength levels
+  int rows;          // LUT keys (24 * n_strength * 3)
+};
+
+// Device-side error word shared by all kernels: first failure wins.
+enum : int { kErrNone = 0, kErrTileOverflow = 1, kErrWaitTimeout = 2, kErrQueue = 3 };
+
+// ------------------------------------------------------------- plane I/O --
+__device__ __forceinline__ float ldp(const float* p) { return __ldg(p); }
+__device__ __forceinline__ float ldp(const __half* p) {
+  return __half2float(__ushort_as_half(__ldg(reinterpret_cast<const unsigned short*>(p))));
+}
+__device__ __forceinline__ void stp(float* p, float v) { *p = v; }
+__device__ __forceinline__ void stp(__half* p, float v) { *p = __float2half_rn(v); }
+// two horizontally adjacent pixels (p must be 2-element aligned)
+__device__ __forceinline__ void stp2(float* p, float a, float b) {
+  *reinterpret_cast<float2*>(p) = make_float2(a, b);
+}
+__device__ __forceinline__ void stp2(__half* p, float a, float b) {
+  *reinterpret_cast<__half2*>(p) = __floats2half2_rn(a, b);
+}
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+__device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
+// GLSL mod(): x - y * floor(x / y)
+__device__ __forceinline__ float gl_mod(float x, float y) { return x - y * floorf(x / y); }
+
+// --------------------------------------------------- structure tensor -----
+// Gradient stencil at grid position p along one axis of an N-tap window:
+// one-sided at the border, central /2 inside, and (FOUR: ravu, ravu-zoom)
+// (-s[p+2] + 8 s[p+1] - 8 s[p-1] + s[p-2]) / 12 where both exist.
+template <int N, bool FOUR, class G>
+__device__ __forceinline__ float deriv(const G& s, int p) {
+  if (p == 0) return s(1) - s(0);
+  if (p == N - 1) return s(N - 1) - s(N - 2);
+  if (FOUR && p >= 2 && p <= N - 3)
+    return (-s(p + 2) + 8.0f * s(p + 1) - 8.0f * s(p - 1) + s(p - 2)) * (1.0f / 12.0f);
+  return (s(p + 1) - s(p - 1)) * 0.5f;
+}
+
+// Gaussian-weighted sum of (gx^2, gx gy, gy^2) over the gradient points:
+// the whole window when N <= 4, else the window minus a one-tap border.
+// `get(kx, ky)` returns the key input at window grid (kx, ky).
+template <int N, bool FOUR, class Get>
+__device__ __forceinline__ void structure_tensor(const Get& get, const KeyParams& kp, float& a,
+                                                 float& b, float& d) {
+  constexpr int P0 = N <= 4 ? 0 : 1;
+  constexpr int P1 = N <= 4 ? N : N - 1;
+  a = 0.0f;
+  b = 0.0f;
+  d = 0.0f;
+  int i = 0;
+#pragma unroll
+  for (int px = P0; px < P1; px++) {
+#pragma unroll
+    for (int py = P0; py < P1; py++) {
+      float gx = deriv<N, FOUR>([&](int q) { return get(q, py); }, px);
+      float gy = deriv<N, FOUR>([&](int q) { return get(px, q); }, py);
+      float w = kp.gw[i++];
+      a += gx * gx * w;
+      b += gx * gy * w;
+      d += gy * gy * w;
+    }
+  }
+}
+
+// Eigen analysis + quantisation -> raw key (not clamped to the LUT).
+// ravu-lite-r3.hook:77-88 (strength thresholds), ravu-r3.hook:121-125 (log2).
+__device__ __forceinline__ int ravu_key(float a, float b, float d, const KeyParams& kp) {
+  float T = a + d, D = a * d - b * b;
+  float delta = sqrtf(fmaxf(T * T / 4.0f - D, 0.0f));
+  float L1 = T / 2.0f + delta, L2 = T / 2.0f - delta;
+  float sqrtL1 = sqrtf(L1), sqrtL2 = sqrtf(L2);  // NaN for L2 < 0, as in GLSL
+  float theta = fabsf(b) < kFltEps ? 0.0f : gl_mod(atan2f(L1 - a, b) + kPi, kPi);
+  float lambda = sqrtL1;
+  float ssum = sqrtL1 + sqrtL2;
+  float mu = ssum < kFltEps ? 0.0f : (sqrtL1 - sqrtL2) / ssum;  // NaN stays NaN
+  float angle = floorf(theta * 24.0f / kPi);
+  float strength;
+  if (kp.log2_mode) {
+    strength = clampf(floorf(log2f(lambda * kp.log2_scale + kFltEps)), 0.0f, kp.log2_max);
+  } else if (kp.n_thr == 3) {
+    strength = lambda >= kp.thr[1] ? (lambda >= kp.thr[2] ? 3.0f : 2.0f) : (lambda >= kp.thr[0] ? 1.0f : 0.0f);
+  } else {
+    strength = lambda >= kp.thr[1] ? 2.0f : (lambda >= kp.thr[0] ? 1.0f : 0.0f);
+  }
+  float coherence = mu >= kp.coh1 ? 2.0f : (mu >= kp.coh0 ? 1.0f : 0.0f);
+  return (int)((angle * (float)kp.n_strength + strength) * 3.0f + coherence);
+}
+
+// Anti-ringing powers: (0.1+v)^32, ^33 and (1.1-v)^32, ^33 by 5 squarings
+// (ravu-lite-ar-r3.hook:91-98).
+struct ArPow {
+  float h32, h33, l32, l33;
+};
+__device__ __forceinline__ ArPow ar_pow(float v) {
+  float h = 0.1f + v, l = 1.1f - v;
+  float h32 = h, l32 = l;
+#pragma unroll
+  for (int i = 0; i < 5; i++) {
+    h32 *= h32;
+    l32 *= l32;
+  }
+  return {h32, h32 * h, l32, l32 * l};
+}
+
+// lo = 1.1 - lo2/lo; hi = hi2/hi - 0.1; mix(res, clamp(res, lo, hi), s)
+__device__ __forceinline__ float ar_finish(float res, float lo, float hi, float lo2, float hi2, float s) {
+  float lob = 1.1f - lo2 / lo;
+  float hib = hi2 / hi - 0.1f;
+  float c = fminf(fmaxf(res, lob), hib);
+  return res * (1.0f - s) + c * s;
+}
+
+// Rec.709 luma of an RGB sample (ravu-r2-rgb.hook:21 color_primary).
+__device__ __forceinline__ float rgb_luma(float r, float g, float b) {
+  return r * 0.2126f + g * 0.7152f + b * 0.0722f;
+}
+
+}  // namespace pz

@@ -99,3 +99,111 @@ def frame(h: int, w: int, seed: int, channels: str = "luma") -> np.ndarray:
     if channels == "yuv":
         return yuv_frame(h, w, seed)
     raise ValueError(channels)
+
+
+# ------------------------------------------------------------------ models --
+
+_WHEN_2X = "HOOKED.w OUTPUT.w / 0.707106 < HOOKED.h OUTPUT.h / 0.707106 < *"
+_WHEN_3X = "HOOKED.w OUTPUT.w / 0.471404 < HOOKED.h OUTPUT.h / 0.471404 < *"
+_WHEN_ZOOM = "HOOKED.w OUTPUT.w < HOOKED.h OUTPUT.h < *"
+
+
+def _parse_name(name: str):
+    import re
+    m = re.fullmatch(r"nnedi3-nns(\d+)-win8x([46])", name)
+    if m:
+        return {"family": "nnedi3", "nns": int(m.group(1)), "win_h": int(m.group(2))}
+    m = re.fullmatch(r"ravu(-lite|-zoom|-3x)?(-ar)?-r([234])(?:-(yuv|rgb))?", name)
+    if not m:
+        raise ValueError(f"not a prescaler name: {name!r}")
+    fam = {None: "ravu", "-lite": "lite", "-zoom": "zoom", "-3x": "3x"}[m.group(1)]
+    return {"family": fam, "ar": 0.8 if m.group(2) else 0.0, "radius": int(m.group(3)),
+            "channels": m.group(4) or "luma"}
+
+
+def synthetic_model(name: str, seed: int = 0):
+    """A canonical model with the shapes and structure of the named hook
+    file but seeded random LUT / neuron weights.  For tests and benchmarks
+    on machines without the ``.hook`` files: the CUDA path and the oracle do
+    not depend on the weight values."""
+    from . import geometry as geo
+    from .hookfile import Pass
+    from .models import Nnedi3Model, RavuModel
+
+    info = _parse_name(name)
+    rng = np.random.default_rng(seed + sum(map(ord, name)))
+
+    def mkpass(desc, when, save=None):
+        return Pass(desc=desc, hooks=["LUMA"], binds=["HOOKED"], save=save, width=None, height=None,
+                    offset=None, when=when, components=None, compute=None, body=[], line=0, body_line=0)
+
+    if info["family"] == "nnedi3":
+        nns, wh = info["nns"], info["win_h"]
+        T = 8 * wh
+        A = rng.normal(0.0, 0.15, size=(T, nns))
+        B = rng.normal(0.0, 0.15, size=(T, nns))
+        A -= A.mean(0)
+        B -= B.mean(0)
+        passes = [mkpass(f"NNEDI3 (double_y, nns{nns}, win8x{wh})", "HOOKED.h OUTPUT.h / 0.707106 <", "nnedi3_int"),
+                  mkpass(f"NNEDI3 (combine_y, nns{nns}, win8x{wh})", "HOOKED.h OUTPUT.h / 0.707106 <"),
+                  mkpass(f"NNEDI3 (double_x, nns{nns}, win8x{wh})", "HOOKED.w OUTPUT.w / 0.707106 <", "nnedi3_int"),
+                  mkpass(f"NNEDI3 (combine_x, nns{nns}, win8x{wh})", "HOOKED.w OUTPUT.w / 0.707106 <")]
+        return Nnedi3Model(name=name, nns=nns, win_w=8, win_h=wh,
+                           taps=np.asarray(geo.nnedi3_taps(8, wh), dtype=np.int32),
+                           weights_a=A.astype(np.float32), weights_b=B.astype(np.float32),
+                           bias_a=rng.normal(0, 0.5, nns).astype(np.float32),
+                           bias_b=rng.normal(0, 0.5, nns).astype(np.float32),
+                           passes=passes, style="synthetic", path="<synthetic>")
+    fam, r = info["family"], info["radius"]
+    n = geo.window_size(fam, r)
+    S = n * n
+    if fam == "ravu":
+        strength = ("log2", 2000.0, 8.0)
+    elif fam == "3x":
+        strength = ("thr", (0.005, 0.02))
+    else:
+        strength = ("thr", (0.004, 0.016, 0.05))
+    ns = int(strength[2]) + 1 if strength[0] == "log2" else len(strength[1]) + 1
+    rows = 24 * ns * 3
+    if fam == "lite":
+        w = rng.normal(0.0, 0.05, size=(rows, S, 4)) + np.exp(-rng.random((1, S, 1)) * 3) * 0.1
+        # fold to the paired layout: column c holds tap c, tap S-1-c reads it reversed
+        lut = np.zeros((rows, (S + 1) // 2, 4))
+        for c in range(S // 2):
+            lut[:, c] = w[:, c]
+        lut[:, S // 2] = w[:, S // 2]
+        tot = lut[:, : S // 2].sum(1) + lut[:, : S // 2, ::-1].sum(1) + lut[:, S // 2]
+        lut[:, S // 2] += 1.0 - tot
+    elif fam == "3x":
+        lut = rng.normal(0.0, 0.05, size=(rows, 2 * ((S + 1) // 2), 4))
+        lut[:, S - 1] += 0.5
+        lut[:, S - 2] += 0.5
+    elif fam == "ravu":
+        ncols = (S // 2 + 3) // 4
+        wt = rng.normal(0.0, 0.03, size=(rows, 4 * ncols))
+        wt[:, S // 2:] = 0.0
+        wt[:, : S // 2] += (0.5 - wt[:, : S // 2].sum(1, keepdims=True)) / (S // 2)
+        lut = wt.reshape(rows, ncols, 4)
+    else:  # zoom
+        nb = (S // 2 + 3) // 4
+        lut = rng.normal(0.0, 0.03, size=(rows * 9, 9 * nb, 4)) + 1.0 / S
+    lut = lut.astype(np.float32)
+    lut_ar = None
+    if fam == "zoom" and info["ar"]:
+        lut_ar = (rng.random(lut.shape) * 0.1).astype(np.float32)
+    when = _WHEN_ZOOM if fam == "zoom" else (_WHEN_3X if fam == "3x" else _WHEN_2X)
+    passes = [mkpass(f"synthetic {name}", when)]
+    return RavuModel(name=name, family=fam, radius=r, channels=info["channels"], ar=info["ar"], lut=lut,
+                     lut_ar=lut_ar, grad_weights=np.asarray(geo.grad_weights(fam, r)), strength=strength,
+                     coherence=(0.25, 0.5), passes=passes, style="synthetic", path="<synthetic>",
+                     ar_taps=geo.lite_ar_taps(r) if fam == "lite" and info["ar"] else None)
+
+
+def model_for(name: str):
+    """(HookModel, source): the parsed model from the package cache when
+    present ("parsed"), else :func:`synthetic_model` ("synthetic")."""
+    from .prescaler import HookModel, cached_model
+    try:
+        return cached_model(name), "parsed"
+    except FileNotFoundError:
+        return HookModel(synthetic_model(name)), "synthetic"

@@ -138,9 +138,7 @@ def structure_key(lum: List[np.ndarray], model) -> Dict[str, np.ndarray]:
             nstr = len(ts) + 1
         c0, c1 = model.coherence
         coherence = np.where(mu >= c1, 2.0, np.where(mu >= c0, 1.0, 0.0))
-        rows = 24 * nstr * 3
-        key = (angle * nstr + strength) * 3.0 + coherence
-        key = np.clip(key, 0, rows - 1).astype(np.int64)   # texture clamp-to-edge
+        key = ((angle * nstr + strength) * 3.0 + coherence).astype(np.int64)   # raw, may reach rows
 
         # ---- boundary detection: FP32 rounding bound on each threshold test
         E = FP32_BUDGET * T + 1e-30
@@ -161,7 +159,12 @@ def structure_key(lum: List[np.ndarray], model) -> Dict[str, np.ndarray]:
             bnd |= np.abs(mu - c) <= dmu + 1e-9
         bnd |= np.abs(ssum * ssum - FLT_EPS * FLT_EPS) <= 2.0 * E
         bnd &= T > 0.0        # a flat window is exact in any precision
-    return {"key": key, "boundary": bnd, "theta": theta, "lambda": lam, "mu": mu}
+    return {"key": key, "boundary": bnd, "theta": theta, "lambda": lam, "mu": mu, "rows": 24 * nstr * 3}
+
+
+def _row(key: np.ndarray, rows: int) -> np.ndarray:
+    """NEAREST LUT row of a key: ``(key + 0.5) / rows`` clamped to the edge."""
+    return np.clip(key, 0, rows - 1)
 
 
 def _ar_powers(v):
@@ -209,6 +212,7 @@ def ravu_lite(model, planes, keys: Optional[np.ndarray] = None):
     lum = [_fetch(p, yy + (k % n + lo), xx + (k // n + lo)) for k in range(S)]
     info = structure_key(lum, model)
     key = info["key"] if keys is None else np.asarray(keys, dtype=np.int64).reshape(H, W)
+    key = _row(key, info["rows"])
     lut = np.asarray(model.lut, dtype=np.float64)          # [rows][cols][4]
     res = np.zeros((4, H, W))
     ar = float(model.ar)
@@ -262,6 +266,7 @@ def ravu_3x(model, planes, keys: Optional[np.ndarray] = None):
     lum = [_luma(v, model.channels) for v in vals]
     info = structure_key(lum, model)
     key = info["key"] if keys is None else np.asarray(keys, dtype=np.int64).reshape(H, W)
+    key = _row(key, info["rows"])
     lut = np.asarray(model.lut, dtype=np.float64)
     res0 = np.zeros((C, 4, H, W))
     res1 = np.zeros((C, 4, H, W))
@@ -316,6 +321,7 @@ def _ravu_pass(model, vals, keys_forced):
     lum = [_luma(v, model.channels) for v in vals]
     info = structure_key(lum, model)
     key = info["key"] if keys_forced is None else keys_forced
+    key = _row(key, info["rows"])
     lut = np.asarray(model.lut, dtype=np.float64).reshape(model.lut.shape[0], -1)   # [rows][4*cols]
     res = np.zeros_like(vals[0])
     for i in range(S // 2):
@@ -323,12 +329,15 @@ def _ravu_pass(model, vals, keys_forced):
     return np.clip(res, 0.0, 1.0), info
 
 
-def ravu_lattice(model, planes, keys: Optional[np.ndarray] = None):
+def ravu_lattice(model, planes, keys: Optional[np.ndarray] = None, int11: Optional[np.ndarray] = None):
     """2x ravu (luma/yuv/rgb), all four passes of ``ravu-r3.hook``.
 
     Output pixel (2i, 2j) is the input, (2i+1, 2j) int10, (2i, 2j+1) int01,
     (2i+1, 2j+1) int11 (``ravu-r3.hook:424-437`` with ``OFFSET -0.5 -0.5``).
     ``keys`` (optional) is ``[3][H][W]``: int11, int10, int01 rows.
+    ``int11`` (optional, ``[C][H][W]``) replaces the computed int11 plane as
+    the input of the two lattice passes, so that they can be checked on
+    exactly the int11 values another implementation produced.
     """
     x = _as_planes(planes)
     C, H, W = x.shape
@@ -339,7 +348,11 @@ def ravu_lattice(model, planes, keys: Optional[np.ndarray] = None):
     yy, xx = np.mgrid[0:H, 0:W]
     kf = None if keys is None else np.asarray(keys, dtype=np.int64).reshape(3, H, W)
     vals = [_fetch(x, yy + (k % n + lo), xx + (k // n + lo)) for k in range(S)]
-    int11, i11 = _ravu_pass(model, vals, None if kf is None else kf[0])
+    own11, i11 = _ravu_pass(model, vals, None if kf is None else kf[0])
+    if int11 is None:
+        src11 = own11
+    else:
+        src11 = np.asarray(int11, dtype=np.float64).reshape(C, H, W)
     out_keys = [i11["key"]]
     bnd = [i11["boundary"]]
     results = {}
@@ -347,7 +360,7 @@ def ravu_lattice(model, planes, keys: Optional[np.ndarray] = None):
         vals = []
         for k in range(S):
             src, dx, dy = _lattice_source(n, k, lattice)
-            vals.append(_fetch(x if src == 0 else int11, yy + dy, xx + dx))
+            vals.append(_fetch(x if src == 0 else src11, yy + dy, xx + dx))
         results[lattice], inf = _ravu_pass(model, vals, None if kf is None else kf[li])
         out_keys.append(inf["key"])
         bnd.append(inf["boundary"])
@@ -355,7 +368,7 @@ def ravu_lattice(model, planes, keys: Optional[np.ndarray] = None):
     out[:, 0::2, 0::2] = x
     out[:, 0::2, 1::2] = results["int10"]
     out[:, 1::2, 0::2] = results["int01"]
-    out[:, 1::2, 1::2] = int11
+    out[:, 1::2, 1::2] = own11
     return out, {"key": np.stack(out_keys), "boundary": np.stack(bnd)}
 
 
@@ -391,13 +404,15 @@ def ravu_zoom(model, planes, out_w: int, out_h: int, keys: Optional[np.ndarray] 
     n = 2 * r
     lo = -(r - 1)
     S = n * n
-    Y, X = np.mgrid[0:out_h, 0:out_w].astype(np.float64)
-    posx = (X + 0.5) / out_w * W
-    posy = (Y + 0.5) / out_h * H
-    spx = (posx - 0.5) - np.floor(posx - 0.5)
-    spy = (posy - 0.5) - np.floor(posy - 0.5)
-    ix = np.floor(posx - 0.5).astype(np.int64)
-    iy = np.floor(posy - 0.5).astype(np.int64)
+    Y, X = np.mgrid[0:out_h, 0:out_w]
+    # pos - 0.5 = ((2X+1) W - OW) / (2 OW), taken exactly: anchor = floor,
+    # subpix = fract (ravu-zoom-r2.hook:25-27)
+    numx = (2 * X.astype(np.int64) + 1) * W - out_w
+    numy = (2 * Y.astype(np.int64) + 1) * H - out_h
+    ix = numx // (2 * out_w)
+    iy = numy // (2 * out_h)
+    spx = (numx - ix * 2 * out_w) / (2.0 * out_w)
+    spy = (numy - iy * 2 * out_h) / (2.0 * out_h)
     vals = [_fetch(x, iy + (k % n + lo), ix + (k // n + lo)) for k in range(S)]
     lum = [_luma(v, model.channels) for v in vals]
     info = structure_key(lum, model)
@@ -430,15 +445,16 @@ def ravu_zoom(model, planes, out_w: int, out_h: int, keys: Optional[np.ndarray] 
     return res, info
 
 
-def keyed_upscale(model, planes, out_size: Optional[Tuple[int, int]] = None, keys=None):
-    """Dispatch on the model family; ``out_size`` = (w, h) for ravu-zoom."""
+def keyed_upscale(model, planes, out_size: Optional[Tuple[int, int]] = None, keys=None, int11=None):
+    """Dispatch on the model family; ``out_size`` = (w, h) for ravu-zoom;
+    ``int11`` overrides the int11 plane fed to the ravu lattice passes."""
     fam = model.family
     if fam == "lite":
         return ravu_lite(model, planes, keys)
     if fam == "3x":
         return ravu_3x(model, planes, keys)
     if fam == "ravu":
-        return ravu_lattice(model, planes, keys)
+        return ravu_lattice(model, planes, keys, int11)
     if fam == "zoom":
         if out_size is None:
             raise ValueError("ravu-zoom needs an output size")

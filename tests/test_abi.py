@@ -1,0 +1,55 @@
+"""The C-ABI library builds, loads and exports every declared entry point
+(no device calls: this runs without a GPU)."""
+import os
+import re
+
+import pytest
+
+from mpv_prescalers_gb300 import _ffi
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(REPO, "include", "prescale.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(_ffi.LIB_PATH):
+        from mpv_prescalers_gb300 import build
+        build.build()
+    return _ffi.lib()
+
+
+def declared():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(pz_[a-z_]+)\s*\(", text)))
+
+
+def test_header_declares_the_entry_points():
+    names = declared()
+    for n in ("pz_model_create", "pz_model_destroy", "pz_run", "pz_last_error", "pz_version",
+              "pz_scratch_bytes", "pz_batch_run", "pz_batch_work_bytes"):
+        assert n in names
+
+
+def test_every_declared_symbol_is_exported(lib):
+    for n in declared():
+        assert hasattr(lib, n), n
+    assert set(_ffi.EXPORTS) >= set(declared()) - set()
+
+
+def test_version_and_error_without_device(lib):
+    assert lib.pz_version() == 1
+    assert isinstance(lib.pz_last_error(), bytes)
+
+
+def test_null_arguments_are_rejected_on_the_host(lib):
+    assert lib.pz_model_create(None, None) == _ffi.PZ_EINVAL
+    assert b"null" in lib.pz_last_error()
+    assert lib.pz_run(None, None, 0, None, 0, None, None) == _ffi.PZ_EINVAL
+
+
+def test_struct_layouts_match_the_header(lib):
+    import ctypes
+    # pz_plane: void* + 4 ints
+    assert ctypes.sizeof(_ffi.Plane) == 8 + 4 * 4
+    assert ctypes.sizeof(_ffi.Opts) >= 4 * 4 + 8 + 8 + 8

@@ -1,0 +1,216 @@
+"""GPU parity: the CUDA path (through the C ABI) against the FP64 oracle.
+
+For every family the plain FP32 form must
+* pick the same LUT key as the oracle for every key evaluation, except keys
+  the oracle flags as sitting on a quantisation boundary (counted), and
+* with the keys it picked, produce pixels within 1e-5 max-abs of the
+  oracle's arithmetic (the oracle re-run with those keys forced).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from mpv_prescalers_gb300 import synth
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+TOL_FP32 = 1e-5          # max-abs, plain FP32 form vs FP64 oracle
+TOL_FP16_MAXABS = 2e-3   # FP16 planes vs oracle on the same FP16-rounded input
+TOL_FP16_PSNR = 55.0
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.fail("CUDA device required for -m gpu tests")
+    yield
+
+
+def _model(name):
+    hm, _src = synth.model_for(name)
+    return hm
+
+
+def _psnr(a, b):
+    mse = float(np.mean((a - b) ** 2))
+    return float("inf") if mse == 0 else 10.0 * np.log10(1.0 / mse)
+
+
+def _run_gpu(hm, x, out_size, dtype=torch.float32, precision="fp32"):
+    xt = torch.from_numpy(np.ascontiguousarray(x)).to("cuda", dtype)
+    y, keys = hm.upscale(xt, out_size=out_size, precision=precision, return_keys=True)
+    torch.cuda.synchronize()
+    return y.float().cpu().numpy().astype(np.float64), keys.cpu().numpy()
+
+
+def _check_keyed(hm, x, out_size, tol=TOL_FP32, dtype=torch.float32):
+    """Keys and values of the GPU against the oracle.
+
+    For the ravu lattice the int10/int01 passes read int11; they are checked
+    on the GPU's own int11 plane so that each pass is compared on identical
+    inputs (the int11 pass itself is checked on the original input).
+    Returns (key mismatches, boundary keys, max-abs with identical keys,
+    PSNR against the unforced oracle).
+    """
+    m = hm.model
+    y, kg = _run_gpu(hm, x, out_size, dtype=dtype)
+    over = y[:, 1::2, 1::2] if m.family == "ravu" else None
+    ref, info = oracle.keyed_upscale(m, x, out_size, int11=over)
+    forced, _ = oracle.keyed_upscale(m, x, out_size, keys=kg, int11=over)
+    assert y.shape == ref.shape
+    err = np.abs(y - forced).max()
+    assert err <= tol, f"{m.name}: max-abs {err:.3e} with identical keys"
+    mism = kg.reshape(info["key"].shape) != info["key"]
+    bad = mism & ~info["boundary"]
+    assert not bad.any(), f"{m.name}: {int(bad.sum())} key mismatches off the quantisation boundary"
+    plain, _ = oracle.keyed_upscale(m, x, out_size)
+    return int(mism.sum()), int(info["boundary"].sum()), err, _psnr(y, plain)
+
+
+LITE = ["ravu-lite-r2", "ravu-lite-r3", "ravu-lite-r4", "ravu-lite-ar-r2", "ravu-lite-ar-r3", "ravu-lite-ar-r4"]
+SIZES = [(37, 45), (16, 64), (1, 1), (3, 5), (9, 33), (144, 256)]
+
+
+@pytest.mark.parametrize("name", LITE)
+@pytest.mark.parametrize("hw", SIZES, ids=lambda s: f"{s[0]}x{s[1]}")
+def test_ravu_lite_fp32(name, hw):
+    hm = _model(name)
+    H, W = hw
+    x = synth.luma_plane(H, W, 11 + H)[None]
+    _check_keyed(hm, x, (2 * W, 2 * H))
+
+
+RAVU = ["ravu-r2", "ravu-r3", "ravu-r4", "ravu-r2-yuv", "ravu-r3-rgb", "ravu-r4-yuv", "ravu-r4-rgb"]
+
+
+@pytest.mark.parametrize("name", RAVU)
+@pytest.mark.parametrize("hw", [(37, 45), (1, 1), (4, 7), (72, 128)], ids=lambda s: f"{s[0]}x{s[1]}")
+def test_ravu_lattice_fp32(name, hw):
+    hm = _model(name)
+    H, W = hw
+    x = synth.frame(H, W, 21 + W, hm.channels)
+    _check_keyed(hm, x, (2 * W, 2 * H))
+
+
+THREE = ["ravu-3x-r2", "ravu-3x-r3", "ravu-3x-r4", "ravu-3x-r3-yuv", "ravu-3x-r2-rgb"]
+
+
+@pytest.mark.parametrize("name", THREE)
+@pytest.mark.parametrize("hw", [(29, 41), (2, 3), (64, 96)], ids=lambda s: f"{s[0]}x{s[1]}")
+def test_ravu_3x_fp32(name, hw):
+    hm = _model(name)
+    H, W = hw
+    x = synth.frame(H, W, 31 + W, hm.channels)
+    _check_keyed(hm, x, (3 * W, 3 * H))
+
+
+ZOOM = ["ravu-zoom-r2", "ravu-zoom-r3", "ravu-zoom-ar-r2", "ravu-zoom-ar-r2-rgb", "ravu-zoom-ar-r2-yuv",
+        "ravu-zoom-r3-rgb", "ravu-zoom-r2-yuv"]
+
+
+@pytest.mark.parametrize("name", ZOOM)
+@pytest.mark.parametrize("geom", [((30, 40), (60, 45)), ((30, 40), (90, 67)), ((17, 23), (40, 39)),
+                                  ((48, 64), (96, 128)), ((2, 3), (5, 7))],
+                         ids=lambda g: f"{g[0][1]}x{g[0][0]}to{g[1][0]}x{g[1][1]}")
+def test_ravu_zoom_fp32(name, geom):
+    hm = _model(name)
+    (H, W), out_size = geom
+    x = synth.frame(H, W, 41 + W, hm.channels)
+    _check_keyed(hm, x, out_size)
+
+
+NN = ["nnedi3-nns16-win8x4", "nnedi3-nns32-win8x6", "nnedi3-nns64-win8x4", "nnedi3-nns128-win8x6",
+      "nnedi3-nns256-win8x4", "nnedi3-nns256-win8x6"]
+
+
+@pytest.mark.parametrize("name", NN)
+@pytest.mark.parametrize("axes", ["y", "x", "yx"])
+def test_nnedi3_fp32(name, axes):
+    hm = _model(name)
+    H, W = 27, 35
+    x = synth.luma_plane(H, W, 51)[None]
+    out_size = (2 * W if "x" in axes else W, 2 * H if "y" in axes else H)
+    xt = torch.from_numpy(x).cuda()
+    y = hm.upscale(xt, out_size=out_size).cpu().numpy().astype(np.float64)
+    ref, info = oracle.nnedi3_upscale(hm.model, x, axes=axes)
+    nb = sum(int(v.sum()) for k, v in info.items() if k.startswith("boundary"))
+    err = np.abs(y - ref)
+    assert nb == 0 or err.max() <= TOL_FP32 or (err > TOL_FP32).sum() <= 64 * nb
+    assert np.median(err) <= TOL_FP32
+    if nb == 0:
+        assert err.max() <= TOL_FP32, f"{name}/{axes}: max-abs {err.max():.3e}"
+
+
+@pytest.mark.parametrize("name", ["ravu-lite-ar-r3", "ravu-lite-ar-r4", "ravu-r3", "ravu-r4-yuv",
+                                  "ravu-zoom-ar-r2-rgb", "ravu-3x-r2"])
+def test_fp16_planes_meet_quality_bar(name):
+    """FP16 planes (FP32 math): against the oracle on the same FP16-rounded
+    input, max-abs <= 2e-3 with the keys the GPU chose, key flips only on
+    the quantisation boundary, PSNR >= 55 dB against the unforced oracle."""
+    hm = _model(name)
+    H, W = 64, 96
+    x = synth.frame(H, W, 61, hm.channels)
+    x16 = x.astype(np.float16).astype(np.float32)
+    out_size = {"zoom": (150, 100), "3x": (3 * W, 3 * H)}.get(hm.family, (2 * W, 2 * H))
+    _mism, _bnd, err, psnr = _check_keyed(hm, x16, out_size, tol=TOL_FP16_MAXABS, dtype=torch.float16)
+    assert psnr >= TOL_FP16_PSNR, f"{name}: PSNR {psnr:.1f} dB"
+
+
+def test_nnedi3_fp16_planes():
+    hm = _model("nnedi3-nns64-win8x4")
+    x = synth.luma_plane(40, 48, 71)[None].astype(np.float16).astype(np.float32)
+    y = hm.upscale(torch.from_numpy(x).to("cuda", torch.float16)).float().cpu().numpy()
+    ref, _ = oracle.nnedi3_upscale(hm.model, x)
+    assert np.abs(y - ref).max() <= TOL_FP16_MAXABS and _psnr(y, ref) >= TOL_FP16_PSNR
+
+
+def test_constant_plane_is_exact_for_nnedi3_and_uses_key_zero():
+    for name in ("ravu-lite-r3", "ravu-r3", "ravu-zoom-r2"):
+        hm = _model(name)
+        c = np.full((1, 20, 30), 0.3125, dtype=np.float32)
+        out_size = (45, 33) if hm.family == "zoom" else (60, 40)
+        _, keys = _run_gpu(hm, c, out_size)
+        assert np.all(keys == 0)
+    hm = _model("nnedi3-nns32-win8x4")
+    y = hm.upscale(torch.full((20, 30), 0.3125, device="cuda"))
+    assert torch.all(y == 0.3125)
+
+
+def test_pitched_planes_match_contiguous():
+    hm = _model("ravu-lite-ar-r3")
+    x = torch.from_numpy(synth.luma_plane(40, 50, 81)).cuda()
+    big = torch.zeros((40, 64), device="cuda")
+    big[:, :50] = x
+    view = big[:, :50]
+    assert view.stride(0) == 64
+    a = hm.upscale(x)
+    b = hm.upscale(view)
+    assert torch.equal(a, b)
+
+
+def test_deterministic_and_translation_equivariant_at_full_size():
+    """1920x1080: two runs are bit-identical, and a crop of the upscaled frame
+    equals the upscale of the cropped input away from the crop border."""
+    hm = _model("ravu-lite-ar-r3")
+    x = torch.from_numpy(synth.luma_plane(1080, 1920, 91)).cuda()
+    a = hm.upscale(x)
+    b = hm.upscale(x)
+    assert torch.equal(a, b)
+    y0, x0, h, w = 301, 517, 200, 300
+    c = hm.upscale(x[y0:y0 + h, x0:x0 + w].contiguous())
+    m = 4  # radius-3 window + margin
+    assert torch.equal(c[2 * m:-2 * m, 2 * m:-2 * m], a[2 * (y0 + m):2 * (y0 + h - m), 2 * (x0 + m):2 * (x0 + w - m)])
+
+
+def test_bad_arguments_raise():
+    from mpv_prescalers_gb300 import PrescaleError
+    hm = _model("ravu-zoom-r2")
+    x = torch.rand((20, 30), device="cuda")
+    with pytest.raises(PrescaleError):
+        hm.run_raw([x], [torch.empty((10, 10), device="cuda")], out_size=(10, 10))  # downscale
+    lite = _model("ravu-lite-r2")
+    with pytest.raises(PrescaleError):
+        lite.run_raw([x], [torch.empty((41, 60), device="cuda")], out_size=(60, 41))  # wrong size
+    with pytest.raises(ValueError):
+        lite.upscale(torch.rand((3, 20, 30), device="cuda"))  # lite is luma only
