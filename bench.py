@@ -349,11 +349,11 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-rows", type=int, default=96, help="input rows per model in the CPU sample")
-    ap.add_argument("--ref-rows", type=int, default=64)
+    ap.add_argument("--cpu-rows", type=int, default=1080, help="input rows per model in the CPU sample")
+    ap.add_argument("--ref-rows", type=int, default=540)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
