@@ -10,21 +10,7 @@
 
 #include "../../include/prescale.h"
 #include "kernels.h"
-
-struct pz_model {
-  int family = 0, radius = 0, channels = 0;
-  float ar = 0.0f;
-  float4* d_lut = nullptr;
-  float4* d_lut_ar = nullptr;
-  int lut_rows = 0, lut_cols = 0;
-  pz::KeyParams kp{};
-  int nns = 0, win_w = 0, win_h = 0;
-  float* d_wts = nullptr;   // [nns][2][T]
-  float* d_cs = nullptr;    // [nns][2]
-  float* d_bias = nullptr;  // [nns][2]
-  __half* d_wts_h = nullptr;
-  int device = 0;
-};
+#include "model.h"
 
 namespace {
 
@@ -77,6 +63,16 @@ int check_plane(const pz_plane& p, const char* what, int idx, bool pairs) {
 }  // namespace
 
 namespace pz {
+int set_error(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
 int* device_error_word() {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
