@@ -150,6 +150,27 @@ size_t pz_batch_work_bytes(const pz_job* jobs, int n_jobs);
 int pz_batch_run(const pz_job* jobs, int n_jobs, void* work, size_t work_bytes,
                  void* cuda_stream);
 
+/* ---- NNEDI3 without any allocation ------------------------------------
+ * No counterpart in the reference: there, the mpv host owns every GPU
+ * buffer.  It exists for hosts that cannot allocate device memory while a
+ * frame is being rendered: a render callback against a display deadline, a
+ * host that hands the library a fixed memory budget up front, or a caller
+ * whose own allocator must not be re-entered.
+ *
+ * Same contract as pz_run for an NNEDI3 model (one luma plane in, one out),
+ * but the row-doubled plane between the row and column passes comes from a
+ * static device array of PZ_STATIC_SCRATCH_BYTES inside the library, and the
+ * call allocates nothing.  Doubling both axes needs 2 * width * height *
+ * element size bytes there (a 1920x1080 FP32 frame fits); larger frames are
+ * rejected with PZ_EINVAL.  Every GPU that loads the library holds the array
+ * until the process exits.  The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress); make that call before any
+ * stream capture.  All calls share the array, so calls that overlap on the
+ * GPU race on it: order them on one stream or with events. */
+#define PZ_STATIC_SCRATCH_BYTES (16u * 1024u * 1024u)
+int pz_nnedi3_run_static(const pz_model* model, const pz_plane* in, pz_plane* out,
+                         const pz_opts* opts, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -79,7 +79,12 @@ EXPORTS = {
     "pz_batch_work_bytes": (ctypes.c_size_t, [ctypes.POINTER(Job), ctypes.c_int]),
     "pz_batch_run": (ctypes.c_int, [ctypes.POINTER(Job), ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t,
                                     ctypes.c_void_p]),
+    "pz_nnedi3_run_static": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Plane), ctypes.POINTER(Plane),
+                                            ctypes.POINTER(Opts), ctypes.c_void_p]),
 }
+
+# Size of the static intermediate-plane array behind pz_nnedi3_run_static.
+PZ_STATIC_SCRATCH_BYTES = 16 * 1024 * 1024
 
 _lib = None
 _lock = threading.Lock()
