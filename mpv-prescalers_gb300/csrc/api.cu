@@ -131,7 +131,15 @@ int pz_model_create(const pz_model_desc* d, pz_model** out) {
       bias[2 * k] = d->bias_a[k];
       bias[2 * k + 1] = d->bias_b[k];
     }
-    for (size_t i = 0; i < w.size(); i++) wh[i] = __float2half_rn(w[i]);
+    // tensor-core operand B [2*nns][T] FP16: rows 0..nns-1 softmax branch,
+    // nns..2nns-1 Elliott branch, stored as no-swizzle K-major core matrices
+    // (8 rows x 8 halves; K-neighbours 64 halves apart, 8-row groups 8*T apart)
+    for (int r = 0; r < 2 * n; r++) {
+      const int k = r % n, br = r / n;
+      for (int t = 0; t < T; t++)
+        wh[(size_t)(r >> 3) * 8 * T + (t >> 3) * 64 + (r & 7) * 8 + (t & 7)] =
+            __float2half_rn(w[((size_t)k * 2 + br) * T + t]);
+    }
     if ((rc = upload(&m->d_wts, w.data(), w.size() * 4)) || (rc = upload(&m->d_cs, cs.data(), cs.size() * 4)) ||
         (rc = upload(&m->d_bias, bias.data(), bias.size() * 4)) ||
         (rc = upload(&m->d_wts_h, wh.data(), wh.size() * 2))) {

@@ -157,6 +157,39 @@ def test_fp16_planes_meet_quality_bar(name):
     assert psnr >= TOL_FP16_PSNR, f"{name}: PSNR {psnr:.1f} dB"
 
 
+@pytest.mark.parametrize("name", NN)
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float16], ids=["f32planes", "f16planes"])
+@pytest.mark.parametrize("axes", ["y", "x", "yx"])
+def test_nnedi3_tensor_core_fast_form(name, dtype, axes):
+    """precision="fast": FP16 normalised windows x FP16 weights on tcgen05,
+    FP32 accumulation in tensor memory, FP32 epilogue.  Against the FP64
+    oracle (on the same input values): max-abs <= 2e-3 and PSNR >= 55 dB.
+    Odd sizes leave partial 32x4 tiles at the right and bottom edges."""
+    hm = _model(name)
+    H, W = 67, 99
+    x = synth.luma_plane(H, W, 52)[None]
+    if dtype == torch.float16:
+        x = x.astype(np.float16).astype(np.float32)
+    out_size = (2 * W if "x" in axes else W, 2 * H if "y" in axes else H)
+    y = hm.upscale(torch.from_numpy(x).to("cuda", dtype), out_size=out_size, precision="fast")
+    y = y.float().cpu().numpy().astype(np.float64)
+    ref, _ = oracle.nnedi3_upscale(hm.model, x, axes=axes)
+    err = np.abs(y - ref).max()
+    assert err <= TOL_FP16_MAXABS, f"{name}/{axes}: max-abs {err:.3e}"
+    assert _psnr(y, ref) >= TOL_FP16_PSNR
+
+
+def test_nnedi3_fast_form_at_1080p_matches_fp32_form():
+    hm = _model("nnedi3-nns128-win8x6")
+    x = torch.from_numpy(synth.luma_plane(1080, 1920, 53)).cuda()
+    a = hm.upscale(x, precision="fast")
+    b = hm.upscale(x, precision="fp32")
+    d = (a - b).abs()
+    assert d.max().item() <= 2 * TOL_FP16_MAXABS
+    mse = float((d.double() ** 2).mean())
+    assert 10 * np.log10(1.0 / mse) >= TOL_FP16_PSNR
+
+
 def test_nnedi3_fp16_planes():
     hm = _model("nnedi3-nns64-win8x4")
     x = synth.luma_plane(40, 48, 71)[None].astype(np.float16).astype(np.float32)
