@@ -104,6 +104,18 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -233,14 +245,20 @@ __global__ void __launch_bounds__(kThreads) nn_tc_kernel(const __grid_constant__
     const float mterm = mean * invstd;
     float wsum = 0.0f, vsum = 0.0f;
     const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+    constexpr int CH = NNS < 32 ? NNS : 32;  // neurons per TMEM load (x16 or x32 columns)
 #pragma unroll 1
-    for (int c = 0; c < NNS; c += 32) {
+    for (int c = 0; c < NNS; c += CH) {
       float s1[32], s2[32];
-      tmem_ld32(lane_addr + c, s1);
-      tmem_ld32(lane_addr + NNS + c, s2);
+      if (CH == 32) {
+        tmem_ld32(lane_addr + c, s1);
+        tmem_ld32(lane_addr + NNS + c, s2);
+      } else {
+        tmem_ld16(lane_addr + c, s1);
+        tmem_ld16(lane_addr + NNS + c, s2);
+      }
       tmem_wait_ld();
 #pragma unroll
-      for (int j = 0; j < 32; j++) {
+      for (int j = 0; j < CH; j++) {
         const float4 q = aux[c + j];
         const float a = s1[j] + mterm * q.x + q.z;
         const float b = s2[j] + mterm * q.y + q.w;
