@@ -4,7 +4,7 @@
 // where that matters for the key (the quantised LUT row):
 //   structure tensor   ravu-lite-r3.hook:48-76, ravu-r3.hook:58-107
 //   eigen/key          ravu-lite-r3.hook:77-88, ravu-r3.hook:108-125
-// All key math is FP32, IEEE division and square root (no fast-math).
+// All key math is FP32; see ravu_key for how each threshold test is evaluated.
 #pragma once
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -90,27 +90,48 @@ __device__ __forceinline__ void structure_tensor(const Get& get, const KeyParams
   }
 }
 
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));  // NaN for x < 0, as in GLSL
+  return r;
+}
+
 // Eigen analysis + quantisation -> raw key (not clamped to the LUT).
 // ravu-lite-r3.hook:77-88 (strength thresholds), ravu-r3.hook:121-125 (log2).
+//
+// The quantised outputs equal the shader's; only the way each threshold test
+// is evaluated changes, so results can differ only where a quantity lies
+// within FP32 rounding of a threshold (the oracle's boundary keys):
+//   * angle: theta * (24/pi) instead of theta * 24 / pi;
+//   * coherence: mu >= c  <=>  (sqrtL1 - sqrtL2) >= c * (sqrtL1 + sqrtL2),
+//     no division; NaN (L2 < 0) still fails every test -> 0, and the
+//     sqrtL1 + sqrtL2 < eps gate still forces 0;
+//   * log2 strength: floor(log2(v)) is the unbiased exponent of v (> 0).
 __device__ __forceinline__ int ravu_key(float a, float b, float d, const KeyParams& kp) {
   float T = a + d, D = a * d - b * b;
-  float delta = sqrtf(fmaxf(T * T / 4.0f - D, 0.0f));
-  float L1 = T / 2.0f + delta, L2 = T / 2.0f - delta;
-  float sqrtL1 = sqrtf(L1), sqrtL2 = sqrtf(L2);  // NaN for L2 < 0, as in GLSL
-  float theta = fabsf(b) < kFltEps ? 0.0f : gl_mod(atan2f(L1 - a, b) + kPi, kPi);
+  float delta = sqrt_approx(fmaxf(T * T * 0.25f - D, 0.0f));
+  float L1 = T * 0.5f + delta, L2 = T * 0.5f - delta;
+  float sqrtL1 = sqrt_approx(L1), sqrtL2 = sqrt_approx(L2);
+  float theta = 0.0f;
+  if (!(fabsf(b) < kFltEps)) {
+    theta = atan2f(L1 - a, b) + kPi;  // mod(atan(L1 - a, b) + pi, pi), t in [0, 2pi]
+    theta = theta >= kPi ? theta - kPi : theta;
+    theta = theta >= kPi ? theta - kPi : theta;  // t = 2pi exactly -> 0, as mod() gives
+  }
+  float angle = floorf(theta * (24.0f / kPi));
   float lambda = sqrtL1;
-  float ssum = sqrtL1 + sqrtL2;
-  float mu = ssum < kFltEps ? 0.0f : (sqrtL1 - sqrtL2) / ssum;  // NaN stays NaN
-  float angle = floorf(theta * 24.0f / kPi);
   float strength;
   if (kp.log2_mode) {
-    strength = clampf(floorf(log2f(lambda * kp.log2_scale + kFltEps)), 0.0f, kp.log2_max);
+    const float v = lambda * kp.log2_scale + kFltEps;
+    strength = clampf((float)((__float_as_int(v) >> 23) - 127), 0.0f, kp.log2_max);
   } else if (kp.n_thr == 3) {
     strength = lambda >= kp.thr[1] ? (lambda >= kp.thr[2] ? 3.0f : 2.0f) : (lambda >= kp.thr[0] ? 1.0f : 0.0f);
   } else {
     strength = lambda >= kp.thr[1] ? 2.0f : (lambda >= kp.thr[0] ? 1.0f : 0.0f);
   }
-  float coherence = mu >= kp.coh1 ? 2.0f : (mu >= kp.coh0 ? 1.0f : 0.0f);
+  const float ssum = sqrtL1 + sqrtL2, sdif = sqrtL1 - sqrtL2;
+  float coherence = 0.0f;
+  if (!(ssum < kFltEps)) coherence = sdif >= kp.coh1 * ssum ? 2.0f : (sdif >= kp.coh0 * ssum ? 1.0f : 0.0f);
   return (int)((angle * (float)kp.n_strength + strength) * 3.0f + coherence);
 }
 

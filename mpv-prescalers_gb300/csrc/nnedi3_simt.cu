@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(256) nn_simt_kernel(const __grid_constant__ Nn
   for (int t = 0; t < NT; t++) {
     const int dx = t % 8 - 3, dy = t / 8 + DY0;
     const int ox = XP ? dy : dx, oy = XP ? dx : dy;
-    xv[t] = tile[threadIdx.y + oy - OY0][threadIdx.x + ox - OX0];
+    xv[t] = tile[(int)threadIdx.y + oy - OY0][(int)threadIdx.x + ox - OX0];
     sum += xv[t];
   }
   const float mean = sum / (float)NT;
@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(256) nn_simt_kernel(const __grid_constant__ Nn
   }
   const float v = clampf(mean + 5.0f * vsum / wsum * stdv, 0.0f, 1.0f);
   T* out = static_cast<T*>(p.out);
-  const float orig = tile[threadIdx.y - OY0][threadIdx.x - OX0];
+  const float orig = tile[(int)threadIdx.y - OY0][(int)threadIdx.x - OX0];
   if (XP) {
     stp2(out + (size_t)gy * p.out_pitch + 2 * gx, orig, v);
   } else {

@@ -17,8 +17,10 @@
 namespace pz {
 namespace {
 
-template <int CM, typename T, int TW, int TH>
-__device__ __forceinline__ void stage_planes(float (*tile)[TH][TW], float (*ltile)[TW], const RavuArgs& p,
+// Stage the clamp-to-edge tiles of all planes; RGB also gets a Rec.709 luma
+// tile (yuv and luma read their key input from plane 0 directly).
+template <int CM, typename T, int TW, int TH, int LH, int LW>
+__device__ __forceinline__ void stage_planes(float (*tile)[TH][TW], float (*ltile)[LW], const RavuArgs& p,
                                              int x0, int y0) {
   constexpr int C = CM == kLuma ? 1 : 3;
   for (int i = threadIdx.y * 32 + threadIdx.x; i < TW * TH; i += 256) {
@@ -30,7 +32,7 @@ __device__ __forceinline__ void stage_planes(float (*tile)[TH][TW], float (*ltil
       v[c] = ldp(static_cast<const T*>(p.in[c]) + (size_t)gy * p.in_pitch[c] + gx);
       tile[c][ty][tx] = v[c];
     }
-    ltile[ty][tx] = CM == kRgb ? rgb_luma(v[0], v[1], v[2]) : v[0];
+    if (CM == kRgb) ltile[ty][tx] = rgb_luma(v[0], v[1], v[2]);
   }
 }
 
@@ -40,29 +42,39 @@ __global__ void __launch_bounds__(256) int11_kernel(const __grid_constant__ Ravu
   constexpr int N = 2 * R, S = N * N, HALO = R - 1;
   constexpr int TW = 32 + N - 1, TH = 8 + N - 1;
   constexpr int C = CM == kLuma ? 1 : 3;
+  constexpr int LH = CM == kRgb ? TH : 1, LW = CM == kRgb ? TW : 1;
   __shared__ float tile[C][TH][TW];
-  __shared__ float ltile[TH][TW];
+  __shared__ float ltile[LH][LW];
   const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 8;
-  stage_planes<CM, T, TW, TH>(tile, ltile, p, x0 - HALO, y0 - HALO);
+  stage_planes<CM, T, TW, TH, LH, LW>(tile, ltile, p, x0 - HALO, y0 - HALO);
   __syncthreads();
   const int gx = x0 + threadIdx.x, gy = y0 + threadIdx.y;
   if (gx >= p.W || gy >= p.H) return;
   const int tx = threadIdx.x, ty = threadIdx.y;
-  auto lum = [&](int kx, int ky) { return ltile[ty + ky][tx + kx]; };
+  auto lum = [&](int kx, int ky) {
+    return CM == kRgb ? ltile[CM == kRgb ? ty + ky : 0][CM == kRgb ? tx + kx : 0] : tile[0][ty + ky][tx + kx];
+  };
   float a, b, d;
   structure_tensor<N, true>(lum, p.kp, a, b, d);
   int key = ravu_key(a, b, d, p.kp);
   if (p.keys) p.keys[(size_t)gy * p.W + gx] = key;
-  const float* L = reinterpret_cast<const float*>(p.lut + (size_t)min(max(key, 0), p.lut_rows - 1) * p.lut_cols);
+  const float4* L = p.lut + (size_t)min(max(key, 0), p.lut_rows - 1) * p.lut_cols;
   float res[C];
 #pragma unroll
   for (int c = 0; c < C; c++) res[c] = 0.0f;
 #pragma unroll
-  for (int i = 0; i < S / 2; i++) {
-    float w = __ldg(L + i);
+  for (int q = 0; q < (S / 2 + 3) / 4; q++) {
+    const float4 w4 = __ldg(L + q);
 #pragma unroll
-    for (int c = 0; c < C; c++)
-      res[c] += (tile[c][ty + i % N][tx + i / N] + tile[c][ty + (S - 1 - i) % N][tx + (S - 1 - i) / N]) * w;
+    for (int j = 0; j < 4; j++) {
+      const int i = 4 * q + j;
+      if (i < S / 2) {
+        const float w = j == 0 ? w4.x : (j == 1 ? w4.y : (j == 2 ? w4.z : w4.w));
+#pragma unroll
+        for (int c = 0; c < C; c++)
+          res[c] += (tile[c][ty + i % N][tx + i / N] + tile[c][ty + (S - 1 - i) % N][tx + (S - 1 - i) / N]) * w;
+      }
+    }
   }
 #pragma unroll
   for (int c = 0; c < C; c++) {
@@ -99,12 +111,13 @@ __global__ void __launch_bounds__(256) lattice_kernel(const __grid_constant__ Ra
   constexpr int N = 2 * R, S = N * N;
   constexpr int TW = 32 + N - 1, TH = 8 + N - 1;
   constexpr int C = CM == kLuma ? 1 : 3;
+  constexpr int LH = CM == kRgb ? TH : 1, LW = CM == kRgb ? TW : 1;
   __shared__ float tin[C][TH][TW];   // input, offsets -(R-1) .. R
-  __shared__ float lin[TH][TW];
+  __shared__ float lin[LH][LW];
   __shared__ float t11[C][TH][TW];   // int11, offsets -R .. R-1
-  __shared__ float l11[TH][TW];
+  __shared__ float l11[LH][LW];
   const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 8;
-  stage_planes<CM, T, TW, TH>(tin, lin, p, x0 - (R - 1), y0 - (R - 1));
+  stage_planes<CM, T, TW, TH, LH, LW>(tin, lin, p, x0 - (R - 1), y0 - (R - 1));
   for (int i = threadIdx.y * 32 + threadIdx.x; i < TW * TH; i += 256) {
     int ty = i / TW, tx = i % TW;
     int cx = clampi(x0 - R + tx, 0, p.W - 1), cy = clampi(y0 - R + ty, 0, p.H - 1);
@@ -114,7 +127,7 @@ __global__ void __launch_bounds__(256) lattice_kernel(const __grid_constant__ Ra
       v[c] = ldp(static_cast<const T*>(p.out[c]) + (size_t)(2 * cy + 1) * p.out_pitch[c] + 2 * cx + 1);
       t11[c][ty][tx] = v[c];
     }
-    l11[ty][tx] = CM == kRgb ? rgb_luma(v[0], v[1], v[2]) : v[0];
+    if (CM == kRgb) l11[CM == kRgb ? ty : 0][CM == kRgb ? tx : 0] = rgb_luma(v[0], v[1], v[2]);
   }
   __syncthreads();
   const int gx = x0 + threadIdx.x, gy = y0 + threadIdx.y;
@@ -122,28 +135,37 @@ __global__ void __launch_bounds__(256) lattice_kernel(const __grid_constant__ Ra
   const int tx = threadIdx.x, ty = threadIdx.y;
 #pragma unroll
   for (int L = 0; L < 2; L++) {
-    auto lum = [&](int kx, int ky) {
-      const int k = kx * N + ky;
-      return lat_src<N>(k, L) == 0 ? lin[ty + lat_dy<N>(k, L) + R - 1][tx + lat_dx<N>(k, L) + R - 1]
-                                   : l11[ty + lat_dy<N>(k, L) + R][tx + lat_dx<N>(k, L) + R];
-    };
     auto val = [&](int c, int k) {
       return lat_src<N>(k, L) == 0 ? tin[c][ty + lat_dy<N>(k, L) + R - 1][tx + lat_dx<N>(k, L) + R - 1]
                                    : t11[c][ty + lat_dy<N>(k, L) + R][tx + lat_dx<N>(k, L) + R];
+    };
+    auto lum = [&](int kx, int ky) {
+      const int k = kx * N + ky;
+      if (CM != kRgb) return val(0, k);
+      return lat_src<N>(k, L) == 0
+                 ? lin[CM == kRgb ? ty + lat_dy<N>(k, L) + R - 1 : 0][CM == kRgb ? tx + lat_dx<N>(k, L) + R - 1 : 0]
+                 : l11[CM == kRgb ? ty + lat_dy<N>(k, L) + R : 0][CM == kRgb ? tx + lat_dx<N>(k, L) + R : 0];
     };
     float a, b, d;
     structure_tensor<N, true>(lum, p.kp, a, b, d);
     int key = ravu_key(a, b, d, p.kp);
     if (p.keys) p.keys[(size_t)(1 + L) * p.W * p.H + (size_t)gy * p.W + gx] = key;
-    const float* Lr = reinterpret_cast<const float*>(p.lut + (size_t)min(max(key, 0), p.lut_rows - 1) * p.lut_cols);
+    const float4* Lr = p.lut + (size_t)min(max(key, 0), p.lut_rows - 1) * p.lut_cols;
     float res[C];
 #pragma unroll
     for (int c = 0; c < C; c++) res[c] = 0.0f;
 #pragma unroll
-    for (int i = 0; i < S / 2; i++) {
-      float w = __ldg(Lr + i);
+    for (int q = 0; q < (S / 2 + 3) / 4; q++) {
+      const float4 w4 = __ldg(Lr + q);
 #pragma unroll
-      for (int c = 0; c < C; c++) res[c] += (val(c, i) + val(c, S - 1 - i)) * w;
+      for (int j = 0; j < 4; j++) {
+        const int i = 4 * q + j;
+        if (i < S / 2) {
+          const float w = j == 0 ? w4.x : (j == 1 ? w4.y : (j == 2 ? w4.z : w4.w));
+#pragma unroll
+          for (int c = 0; c < C; c++) res[c] += (val(c, i) + val(c, S - 1 - i)) * w;
+        }
+      }
     }
 #pragma unroll
     for (int c = 0; c < C; c++) {
