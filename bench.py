@@ -221,19 +221,21 @@ def run_gpu(args):
     kern_ms = statistics.mean(a.elapsed_time(b) for a, b in kev)
 
     # ---- end to end: pinned host frames in, upscaled frames back, per step
-    host_in = torch.from_numpy(frames).to(torch.float16).pin_memory()
-    host_out = {n: torch.empty((NFRAMES, 2 * H, 2 * W), dtype=torch.float16).pin_memory() for n in MODELS}
+    host_in = torch.from_numpy(frames).to(torch.float16).unsqueeze(1).pin_memory()
+    host_out = {n: torch.empty((NFRAMES, 1, 2 * H, 2 * W), dtype=torch.float16).pin_memory() for n in MODELS}
 
     def e2e_step():
-        xd = host_in.to(dev, non_blocking=True)
+        # public API on host frames: H2D copy, upscale and D2H copy of frame i
+        # overlap with its neighbours on three streams
         for n in MODELS:
-            y = models[n].upscale(xd.unsqueeze(1))  # public API, [N][C][H][W] frames in, new tensor out
-            host_out[n].copy_(y.squeeze(1), non_blocking=True)
+            models[n].upscale_host(host_in, out=host_out[n])
 
     for _ in range(args.warmup):
         e2e_step()
     torch.cuda.synchronize()
     barrier()
+    # upscale_host returns when the frames are back in host memory; the two
+    # events on the default stream bracket that wall time
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)

@@ -142,11 +142,26 @@ typedef struct {
   pz_opts opts;
 } pz_job;
 
-/* Run many jobs (any mix of RAVU models, any frame sizes) in one persistent
- * launch over a device work queue of tiles.  Jobs whose chain needs more
- * than one dependent pass (ravu lattice, nnedi3) are run as phases.
- * `work` is caller device memory of at least pz_batch_work_bytes(). */
+/* Many frames of many models per launch (replaces the back-to-back shader
+ * dispatches a multi-stream host issues).  RAVU jobs of any mix and frame
+ * size run as one persistent kernel per plane dtype whose CTAs pull 32x8
+ * tiles of every job from a device counter; the ravu lattice pass follows as
+ * a second persistent kernel (it reads the int11 values of the first);
+ * NNEDI3 jobs run as their own stream-ordered passes.  `work` is caller
+ * device memory of at least pz_batch_work_bytes(); it holds the job table
+ * and the tile counters and must stay in place while the plan is used.
+ *
+ * pz_batch_create validates the jobs and uploads the table (synchronous on
+ * `cuda_stream`); pz_batch_launch only enqueues a memset and kernels, so it
+ * can be captured into a CUDA graph and replayed while the jobs' buffers
+ * stay in place; pz_batch_run is create + launch + destroy.  ctas_per_sm
+ * caps the persistent grid (0 = as many as fit). */
+typedef struct pz_batch pz_batch;
 size_t pz_batch_work_bytes(const pz_job* jobs, int n_jobs);
+int pz_batch_create(const pz_job* jobs, int n_jobs, void* work, size_t work_bytes,
+                    int ctas_per_sm, void* cuda_stream, pz_batch** out);
+int pz_batch_launch(const pz_batch* plan, void* cuda_stream);
+void pz_batch_destroy(pz_batch* plan);
 int pz_batch_run(const pz_job* jobs, int n_jobs, void* work, size_t work_bytes,
                  void* cuda_stream);
 

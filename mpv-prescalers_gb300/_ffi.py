@@ -77,6 +77,10 @@ EXPORTS = {
     "pz_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Plane), ctypes.c_int, ctypes.POINTER(Plane),
                               ctypes.c_int, ctypes.POINTER(Opts), ctypes.c_void_p]),
     "pz_batch_work_bytes": (ctypes.c_size_t, [ctypes.POINTER(Job), ctypes.c_int]),
+    "pz_batch_create": (ctypes.c_int, [ctypes.POINTER(Job), ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t,
+                                       ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "pz_batch_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "pz_batch_destroy": (None, [ctypes.c_void_p]),
     "pz_batch_run": (ctypes.c_int, [ctypes.POINTER(Job), ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t,
                                     ctypes.c_void_p]),
     "pz_nnedi3_run_static": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Plane), ctypes.POINTER(Plane),

@@ -1,0 +1,253 @@
+"""Batched execution: many frames of many models per launch.
+
+``Batch`` binds a fixed list of jobs (model, input planes, output planes) to
+a ``pz_batch`` plan (``include/prescale.h``): RAVU jobs of every model and
+frame size run as one persistent kernel per plane dtype pulling 32x8 tiles
+from a device counter (plus a second one for the ravu lattice pass); NNEDI3
+jobs run as their own passes.  ``Batch.capture()`` records the whole launch
+into a CUDA graph so that a steady-state batch costs one graph replay.
+
+``autotune(jobs)`` times the execution strategies of a batch -- one launch
+per frame, or the persistent kernel with 1, 2 or as many CTAs per SM as fit
+-- on the live device and caches the winner per GPU and batch signature in
+a JSON plan cache.
+"""
+from __future__ import annotations
+
+import ctypes
+import hashlib
+import json
+import os
+import threading
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional, Sequence, Tuple
+
+from . import _ffi
+from .prescaler import PRECISIONS, HookModel
+
+
+def _torch():
+    import torch
+    return torch
+
+
+@dataclass
+class Job:
+    """One frame through one model: planes are lists of [H][W] CUDA tensors."""
+    model: HookModel
+    inputs: List["torch.Tensor"]
+    outputs: List["torch.Tensor"]
+    out_size: Optional[Tuple[int, int]] = None
+    precision: str = "fp32"
+    scratch: Optional["torch.Tensor"] = None
+
+    @staticmethod
+    def make(model: HookModel, frame, out_size=None, precision="fp32", out=None) -> "Job":
+        """A job for ``frame`` ([H][W] or [C][H][W] CUDA tensor); allocates
+        the outputs (and NNEDI3 scratch) unless ``out`` is given."""
+        torch = _torch()
+        pl = [frame] if frame.dim() == 2 else list(frame.unbind(0))
+        H, W = pl[0].shape
+        OW, OH = model.output_size(W, H, out_size)
+        if out is None:
+            outs = [torch.empty((OH, OW), dtype=pl[0].dtype, device=pl[0].device) for _ in pl]
+        else:
+            outs = [out] if out.dim() == 2 else list(out.unbind(0))
+        scratch = None
+        if model.family == "nnedi3" and model.nnedi3_axes(W, H, (OW, OH)) == 3:
+            scratch = torch.empty(2 * H * W * pl[0].element_size(), dtype=torch.uint8, device=pl[0].device)
+        return Job(model, pl, outs, (OW, OH), precision, scratch)
+
+    def signature(self) -> Tuple:
+        p = self.inputs[0]
+        return (self.model.name, p.shape[1], p.shape[0], self.out_size, str(p.dtype), self.precision)
+
+    def to_c(self) -> _ffi.Job:
+        torch = _torch()
+        j = _ffi.Job()
+        j.model = self.model.device_handle(self.inputs[0].device.index)
+        dt = _ffi.PZ_F32 if self.inputs[0].dtype == torch.float32 else _ffi.PZ_F16
+        for i, (p, o) in enumerate(zip(self.inputs, self.outputs)):
+            j.inp[i] = _ffi.Plane(p.data_ptr(), p.shape[1], p.shape[0], p.stride(0), dt)
+            j.out[i] = _ffi.Plane(o.data_ptr(), o.shape[1], o.shape[0], o.stride(0), dt)
+        j.n_planes = len(self.inputs)
+        j.opts.precision = PRECISIONS[self.precision]
+        j.opts.out_width, j.opts.out_height = self.out_size
+        if self.model.family == "nnedi3":
+            W, H = self.inputs[0].shape[1], self.inputs[0].shape[0]
+            j.opts.nnedi3_axes = self.model.nnedi3_axes(W, H, self.out_size)
+        if self.scratch is not None:
+            j.opts.scratch = self.scratch.data_ptr()
+            j.opts.scratch_bytes = self.scratch.numel()
+        return j
+
+
+class Batch:
+    """A persistent-launch plan over fixed jobs (their tensors stay bound)."""
+
+    def __init__(self, jobs: Sequence[Job], ctas_per_sm: int = 0, stream=None):
+        torch = _torch()
+        if not jobs:
+            raise ValueError("empty batch")
+        self.jobs = list(jobs)
+        self.device = self.jobs[0].inputs[0].device
+        self._cjobs = (_ffi.Job * len(self.jobs))(*[j.to_c() for j in self.jobs])
+        L = _ffi.lib()
+        nbytes = L.pz_batch_work_bytes(self._cjobs, len(self.jobs))
+        self.work = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=self.device)
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        h = ctypes.c_void_p()
+        _ffi.check(L.pz_batch_create(self._cjobs, len(self.jobs), self.work.data_ptr(), self.work.numel(),
+                                     int(ctas_per_sm), s.cuda_stream, ctypes.byref(h)))
+        self._plan = h.value
+        self.graph = None
+
+    def launch(self, stream=None):
+        torch = _torch()
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        _ffi.check(_ffi.lib().pz_batch_launch(self._plan, s.cuda_stream))
+
+    def capture(self):
+        """Record one launch into a CUDA graph (call launch() once first so
+        every kernel is loaded and configured)."""
+        torch = _torch()
+        s = torch.cuda.Stream(self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(s):
+            g.capture_begin()
+            self.launch(stream=s)
+            g.capture_end()
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        self.graph = g
+        return g
+
+    def replay(self):
+        if self.graph is None:
+            self.capture()
+        self.graph.replay()
+
+    def close(self):
+        if getattr(self, "_plan", None):
+            _ffi.lib().pz_batch_destroy(self._plan)
+            self._plan = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def run_per_job(jobs: Sequence[Job], stream=None):
+    """The unbatched strategy: one pz_run chain per job."""
+    for j in jobs:
+        j.model.run_raw(j.inputs, j.outputs, out_size=j.out_size, precision=j.precision, stream=stream,
+                        scratch=j.scratch)
+
+
+# ------------------------------------------------------------ autotuner ----
+
+STRATEGIES = ("per_job", "batch:1", "batch:2", "batch:0")
+
+
+def _default_cache_path() -> str:
+    base = os.environ.get("PRESCALER_PLAN_CACHE")
+    if base:
+        return base
+    return os.path.join(os.path.expanduser("~"), ".cache", "mpv_prescalers_gb300", "plans.json")
+
+
+class PlanCache:
+    """Tuned strategies, keyed by GPU name and batch signature (JSON file)."""
+
+    def __init__(self, path: Optional[str] = None):
+        self.path = path or _default_cache_path()
+        self._lock = threading.Lock()
+        self.entries: Dict[str, dict] = {}
+        try:
+            with open(self.path) as f:
+                self.entries = json.load(f)
+        except (OSError, ValueError):
+            self.entries = {}
+
+    @staticmethod
+    def key(gpu: str, jobs: Sequence[Job]) -> str:
+        sig = json.dumps(sorted(str(j.signature()) for j in jobs))
+        return gpu + ":" + hashlib.sha1(sig.encode()).hexdigest()[:16]
+
+    def get(self, key: str) -> Optional[dict]:
+        return self.entries.get(key)
+
+    def put(self, key: str, value: dict) -> None:
+        with self._lock:
+            self.entries[key] = value
+            try:
+                os.makedirs(os.path.dirname(self.path), exist_ok=True)
+                tmp = self.path + ".tmp"
+                with open(tmp, "w") as f:
+                    json.dump(self.entries, f, indent=1, sort_keys=True)
+                os.replace(tmp, self.path)
+            except OSError:
+                pass  # a read-only cache location only loses persistence
+
+
+def _time_ms(fn, reps: int) -> float:
+    torch = _torch()
+    fn()
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def autotune(jobs: Sequence[Job], cache: Optional[PlanCache] = None, reps: int = 5,
+             strategies: Sequence[str] = STRATEGIES) -> Tuple[str, Dict[str, float]]:
+    """Pick the fastest strategy for this batch on this GPU (cached)."""
+    torch = _torch()
+    cache = cache or PlanCache()
+    gpu = torch.cuda.get_device_name(jobs[0].inputs[0].device)
+    key = PlanCache.key(gpu, jobs)
+    hit = cache.get(key)
+    if hit and hit.get("strategy") in strategies:
+        return hit["strategy"], hit.get("times_ms", {})
+    times = {}
+    for st in strategies:
+        if st == "per_job":
+            times[st] = _time_ms(lambda: run_per_job(jobs), reps)
+        else:
+            b = Batch(jobs, ctas_per_sm=int(st.split(":")[1]))
+            times[st] = _time_ms(b.launch, reps)
+            b.close()
+    best = min(times, key=times.get)
+    cache.put(key, {"strategy": best, "times_ms": times})
+    return best, times
+
+
+class Executor:
+    """Runs a fixed batch with its tuned strategy, replaying a CUDA graph."""
+
+    def __init__(self, jobs: Sequence[Job], cache: Optional[PlanCache] = None, tune: bool = True,
+                 use_graph: bool = True):
+        self.jobs = list(jobs)
+        self.strategy = autotune(self.jobs, cache)[0] if tune else "batch:0"
+        self.batch = None
+        self.graph = None
+        if self.strategy != "per_job":
+            self.batch = Batch(self.jobs, ctas_per_sm=int(self.strategy.split(":")[1]))
+            if use_graph:
+                self.batch.launch()
+                self.batch.capture()
+
+    def run(self):
+        if self.batch is None:
+            run_per_job(self.jobs)
+        elif self.batch.graph is not None:
+            self.batch.replay()
+        else:
+            self.batch.launch()

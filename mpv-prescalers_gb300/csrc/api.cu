@@ -346,6 +346,7 @@ int pz_run(const pz_model* m, const pz_plane* in, int n_in, pz_plane* out, int n
     a.lut_cols = m->lut_cols;
     a.ar = m->ar;
     a.keys = o ? o->keys : nullptr;
+    a.err = pz::device_error_word();
     a.kp = m->kp;
     switch (m->family) {
       case PZ_RAVU_LITE: rc = pz::launch_lite(a, m->radius, m->ar != 0.0f, dt, s); break;
@@ -359,21 +360,6 @@ int pz_run(const pz_model* m, const pz_plane* in, int n_in, pz_plane* out, int n
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
   return PZ_OK;
-}
-
-size_t pz_batch_work_bytes(const pz_job* jobs, int n_jobs) {
-  (void)jobs;
-  (void)n_jobs;
-  return 0;
-}
-
-int pz_batch_run(const pz_job* jobs, int n_jobs, void* work, size_t work_bytes, void* stream) {
-  (void)jobs;
-  (void)n_jobs;
-  (void)work;
-  (void)work_bytes;
-  (void)stream;
-  return fail(PZ_ENOTSUP, "batched execution not built yet");
 }
 
 }  // extern "C"

@@ -1,0 +1,17 @@
+// Persistent batch kernel, __half planes.
+#include "batch_kernel.cuh"
+
+namespace pz {
+
+int launch_batch_f16(const DevJob* jobs, int n_jobs, int total, int* counter, int grid, cudaStream_t s) {
+  batch_kernel<__half><<<grid, kTileThreads, kBatchSmem, s>>>(jobs, n_jobs, total, counter);
+  return 0;
+}
+
+int batch_fit_f16() {
+  int fit = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, batch_kernel<__half>, kTileThreads, kBatchSmem);
+  return fit;
+}
+
+}  // namespace pz

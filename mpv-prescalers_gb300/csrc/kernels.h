@@ -23,6 +23,7 @@ struct RavuArgs {
   int lut_rows, lut_cols;
   float ar;
   int32_t* keys;     // optional raw-key output
+  int* err;          // device error word (kErr*)
   KeyParams kp;
 };
 

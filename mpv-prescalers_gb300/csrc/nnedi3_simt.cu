@@ -98,9 +98,14 @@ template <int WH, bool XP, typename T>
 int launch_one(const NnArgs& a, cudaStream_t s) {
   const size_t smem = ((size_t)a.nns * 2 * 8 * WH + (size_t)a.nns * 4) * sizeof(float);
   auto kern = nn_simt_kernel<WH, XP, T>;
-  if (smem > 48 * 1024) {
+  static size_t configured[64] = {};  // largest dynamic smem enabled, per device
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return -95;
+  if (smem > 48 * 1024 && smem > configured[dev]) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return -5;
+    configured[dev] = smem;
   }
   dim3 blk(32, 8), grd((a.W + 31) / 32, (a.H + 7) / 8);
   kern<<<grd, blk, smem, s>>>(a);

@@ -1,0 +1,513 @@
+// RAVU tile programs: one 256-thread CTA computes one tile of outputs.
+//
+// Each program is a struct with the shared-memory bytes it needs and a
+// device `run(p, x0, y0, smem)` that stages the tile (plus its radius halo)
+// and computes it.  The per-model kernels (ravu_lite.cu, ravu_lattice.cu,
+// ravu_zoom.cu) launch one CTA per tile; the persistent batch kernel
+// (batch.cu) feeds many programs of many frames to the same CTAs.
+//
+// References (per program):
+//   LiteTile    compute/ravu-lite-ar-r3.hook:15-171, ravu-lite-r3.hook:15-131
+//   ThreeXTile  compute/ravu-3x-r2.hook:15-115
+//   Int11Tile   ravu-r3.hook:15-146 (compute/ravu-r3.hook:15-154)
+//   LatticeTile ravu-r3.hook:148-437 (compute/ravu-r3.hook:155-430)
+//   ZoomTile    ravu-zoom-r2.hook:15-139, compute/ravu-zoom-ar-r2-rgb.hook:15-238
+//
+// Input tiles are 32 x 8 input pixels (zoom: 32 x 8 output pixels); thread
+// t handles column t % 32 of row t / 32.  Out-of-range reads replicate the
+// edge texel (the mpv texture border mode).
+#pragma once
+#include "kernels.h"
+
+namespace pz {
+
+constexpr int kTileW = 32, kTileH = 8, kTileThreads = 256;
+
+__host__ __device__ constexpr int cabs(int v) { return v < 0 ? -v : v; }
+
+// Stage a (TW x TH) clamp-to-edge tile of one plane at origin (x0, y0).
+template <int TW, int TH, typename T>
+__device__ __forceinline__ void stage_tile(float* tile, const T* in, int pitch, int W, int H, int x0, int y0) {
+  for (int i = threadIdx.x; i < TW * TH; i += kTileThreads) {
+    const int ty = i / TW, tx = i % TW;
+    const int gx = clampi(x0 + tx, 0, W - 1), gy = clampi(y0 + ty, 0, H - 1);
+    tile[i] = ldp(in + (size_t)gy * pitch + gx);
+  }
+}
+
+// Stage all planes of a frame; RGB also gets a Rec.709 luma tile (the key
+// input); luma and yuv take their key input from plane 0.
+template <int CM, int TW, int TH, typename T>
+__device__ __forceinline__ void stage_planes(float* tile, float* ltile, const RavuArgs& p, int x0, int y0) {
+  constexpr int C = CM == kLuma ? 1 : 3;
+  for (int i = threadIdx.x; i < TW * TH; i += kTileThreads) {
+    const int ty = i / TW, tx = i % TW;
+    const int gx = clampi(x0 + tx, 0, p.W - 1), gy = clampi(y0 + ty, 0, p.H - 1);
+    float v[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+      v[c] = ldp(static_cast<const T*>(p.in[c]) + (size_t)gy * p.in_pitch[c] + gx);
+      tile[c * TW * TH + i] = v[c];
+    }
+    if (CM == kRgb) ltile[i] = rgb_luma(v[0], v[1], v[2]);
+  }
+}
+
+// ------------------------------------------------------------ ravu-lite ---
+// Does lite LUT column c take part in the anti-ringing sums?  r2: every
+// tap; r3/r4: the 13-tap diamond |dx|+|dy| <= 2 (ravu-lite-ar-r3.hook:93-170).
+template <int R>
+__host__ __device__ constexpr bool lite_ar_col(int c) {
+  return R == 2 || cabs(c / (2 * R - 1) - (R - 1)) + cabs(c % (2 * R - 1) - (R - 1)) <= 2;
+}
+
+template <int R, bool AR, typename T>
+struct LiteTile {
+  static constexpr int N = 2 * R - 1, S = N * N, HALO = R - 1;
+  static constexpr int TW = kTileW + N - 1, TH = kTileH + N - 1;
+  // value tile, then (AR) the anti-ringing powers of every tile value
+  static constexpr size_t smem_bytes = (size_t)((TW * TH + 3) & ~3) * 4 + (AR ? (size_t)TW * TH * 16 : 0);
+
+  __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem) {
+    float* tile = smem;
+    float4* ptile = reinterpret_cast<float4*>(smem + ((TW * TH + 3) & ~3));
+    stage_tile<TW, TH>(tile, static_cast<const T*>(p.in[0]), p.in_pitch[0], p.W, p.H, x0 - HALO, y0 - HALO);
+    __syncthreads();
+    if (AR) {  // (h32, l32, h33, l33) once per value instead of once per window tap
+      for (int i = threadIdx.x; i < TW * TH; i += kTileThreads) {
+        const ArPow q = ar_pow(tile[i]);
+        ptile[i] = make_float4(q.h32, q.l32, q.h33, q.l33);
+      }
+      __syncthreads();
+    }
+    const int tx = threadIdx.x % kTileW, ty = threadIdx.x / kTileW;
+    const int gx = x0 + tx, gy = y0 + ty;
+    if (gx >= p.W || gy >= p.H) return;
+    auto get = [&](int kx, int ky) { return tile[(ty + ky) * TW + tx + kx]; };
+    auto pw = [&](int k) {
+      const float4 q = ptile[(ty + k % N) * TW + tx + k / N];
+      return ArPow{q.x, q.z, q.y, q.w};
+    };
+    float a, b, d;
+    structure_tensor<N, false>(get, p.kp, a, b, d);
+    const int key = ravu_key(a, b, d, p.kp);
+    if (p.keys) p.keys[(size_t)gy * p.W + gx] = key;
+    const float4* L = p.lut + (size_t)min(max(key, 0), p.lut_rows - 1) * p.lut_cols;
+    float4 res = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 hi = res, lo = res, hi2 = res, lo2 = res;
+#pragma unroll
+    for (int c = 0; c < S / 2; c++) {
+      const float4 w = __ldg(L + c);
+      const float va = get(c / N, c % N), vb = get((S - 1 - c) / N, (S - 1 - c) % N);
+      // res += va * w + vb * w.wzyx
+      res.x += va * w.x + vb * w.w;
+      res.y += va * w.y + vb * w.z;
+      res.z += va * w.z + vb * w.y;
+      res.w += va * w.w + vb * w.x;
+      if (AR && lite_ar_col<R>(c)) {
+        const float4 wg = make_float4(fmaxf(w.x, 0.f), fmaxf(w.y, 0.f), fmaxf(w.z, 0.f), fmaxf(w.w, 0.f));
+        const ArPow pa = pw(c), pb = pw(S - 1 - c);
+        hi.x += pa.h32 * wg.x + pb.h32 * wg.w;  hi.y += pa.h32 * wg.y + pb.h32 * wg.z;
+        hi.z += pa.h32 * wg.z + pb.h32 * wg.y;  hi.w += pa.h32 * wg.w + pb.h32 * wg.x;
+        lo.x += pa.l32 * wg.x + pb.l32 * wg.w;  lo.y += pa.l32 * wg.y + pb.l32 * wg.z;
+        lo.z += pa.l32 * wg.z + pb.l32 * wg.y;  lo.w += pa.l32 * wg.w + pb.l32 * wg.x;
+        hi2.x += pa.h33 * wg.x + pb.h33 * wg.w; hi2.y += pa.h33 * wg.y + pb.h33 * wg.z;
+        hi2.z += pa.h33 * wg.z + pb.h33 * wg.y; hi2.w += pa.h33 * wg.w + pb.h33 * wg.x;
+        lo2.x += pa.l33 * wg.x + pb.l33 * wg.w; lo2.y += pa.l33 * wg.y + pb.l33 * wg.z;
+        lo2.z += pa.l33 * wg.z + pb.l33 * wg.y; lo2.w += pa.l33 * wg.w + pb.l33 * wg.x;
+      }
+    }
+    {
+      constexpr int c = S / 2;
+      const float4 w = __ldg(L + c);
+      const float v = get(c / N, c % N);
+      res.x += v * w.x; res.y += v * w.y; res.z += v * w.z; res.w += v * w.w;
+      if (AR) {
+        const float4 wg = make_float4(fmaxf(w.x, 0.f), fmaxf(w.y, 0.f), fmaxf(w.z, 0.f), fmaxf(w.w, 0.f));
+        const ArPow pc = pw(c);
+        hi.x += pc.h32 * wg.x; hi.y += pc.h32 * wg.y; hi.z += pc.h32 * wg.z; hi.w += pc.h32 * wg.w;
+        lo.x += pc.l32 * wg.x; lo.y += pc.l32 * wg.y; lo.z += pc.l32 * wg.z; lo.w += pc.l32 * wg.w;
+        hi2.x += pc.h33 * wg.x; hi2.y += pc.h33 * wg.y; hi2.z += pc.h33 * wg.z; hi2.w += pc.h33 * wg.w;
+        lo2.x += pc.l33 * wg.x; lo2.y += pc.l33 * wg.y; lo2.z += pc.l33 * wg.z; lo2.w += pc.l33 * wg.w;
+      }
+    }
+    if (AR) {  // no [0,1] clamp after anti-ringing (compute/ravu-lite-ar-r3.hook:166)
+      res.x = ar_finish(res.x, lo.x, hi.x, lo2.x, hi2.x, p.ar);
+      res.y = ar_finish(res.y, lo.y, hi.y, lo2.y, hi2.y, p.ar);
+      res.z = ar_finish(res.z, lo.z, hi.z, lo2.z, hi2.z, p.ar);
+      res.w = ar_finish(res.w, lo.w, hi.w, lo2.w, hi2.w, p.ar);
+    } else {
+      res.x = clampf(res.x, 0.f, 1.f); res.y = clampf(res.y, 0.f, 1.f);
+      res.z = clampf(res.z, 0.f, 1.f); res.w = clampf(res.w, 0.f, 1.f);
+    }
+    // res[0..3] -> offsets (0,0), (0,1), (1,0), (1,1)  (compute/ravu-lite-r3.hook:101-104)
+    T* out = static_cast<T*>(p.out[0]);
+    const int op = p.out_pitch[0];
+    stp2(out + (size_t)(2 * gy) * op + 2 * gx, res.x, res.z);
+    stp2(out + (size_t)(2 * gy + 1) * op + 2 * gx, res.y, res.w);
+  }
+};
+
+// --------------------------------------------------------------- ravu-3x --
+template <int R, int CM, typename T>
+struct ThreeXTile {
+  static constexpr int N = 2 * R - 1, S = N * N, HALO = R - 1;
+  static constexpr int TW = kTileW + N - 1, TH = kTileH + N - 1;
+  static constexpr int C = CM == kLuma ? 1 : 3;
+  static constexpr size_t smem_bytes = (size_t)(C + (CM == kRgb ? 1 : 0)) * TW * TH * 4;
+
+  __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem) {
+    float* tile = smem;
+    float* ltile = smem + C * TW * TH;
+    stage_planes<CM, TW, TH, T>(tile, ltile, p, x0 - HALO, y0 - HALO);
+    __syncthreads();
+    const int tx = threadIdx.x % kTileW, ty = threadIdx.x / kTileW;
+    const int gx = x0 + tx, gy = y0 + ty;
+    if (gx >= p.W || gy >= p.H) return;
+    auto val = [&](int c, int t) { return tile[c * TW * TH + (ty + t % N) * TW + tx + t / N]; };
+    auto lum = [&](int kx, int ky) {
+      return CM == kRgb ? ltile[(ty + ky) * TW + tx + kx] : tile[(ty + ky) * TW + tx + kx];
+    };
+    float a, b, d;
+    structure_tensor<N, false>(lum, p.kp, a, b, d);
+    const int key = ravu_key(a, b, d, p.kp);
+    if (p.keys) p.keys[(size_t)gy * p.W + gx] = key;
+    const float4* L = p.lut + (size_t)min(max(key, 0), p.lut_rows - 1) * p.lut_cols;
+    float4 r0[C], r1[C];
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+      r0[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+      r1[c] = r0[c];
+    }
+#pragma unroll
+    for (int t = 0; t < S / 2; t++) {
+      const float4 w0 = __ldg(L + 2 * t), w1 = __ldg(L + 2 * t + 1);
+#pragma unroll
+      for (int c = 0; c < C; c++) {
+        const float va = val(c, t), vb = val(c, S - 1 - t);
+        // res0 += a*w0 + b*w1.wzyx; res1 += a*w1 + b*w0.wzyx
+        r0[c].x += va * w0.x + vb * w1.w; r0[c].y += va * w0.y + vb * w1.z;
+        r0[c].z += va * w0.z + vb * w1.y; r0[c].w += va * w0.w + vb * w1.x;
+        r1[c].x += va * w1.x + vb * w0.w; r1[c].y += va * w1.y + vb * w0.z;
+        r1[c].z += va * w1.z + vb * w0.y; r1[c].w += va * w1.w + vb * w0.x;
+      }
+    }
+    constexpr int tc = S / 2;
+    const float4 w0 = __ldg(L + 2 * tc), w1 = __ldg(L + 2 * tc + 1);
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+      const float v = val(c, tc);
+      r0[c].x += v * w0.x; r0[c].y += v * w0.y; r0[c].z += v * w0.z; r0[c].w += v * w0.w;
+      r1[c].x += v * w1.x; r1[c].y += v * w1.y; r1[c].z += v * w1.z; r1[c].w += v * w1.w;
+      const float4 a0 = make_float4(clampf(r0[c].x, 0.f, 1.f), clampf(r0[c].y, 0.f, 1.f),
+                                    clampf(r0[c].z, 0.f, 1.f), clampf(r0[c].w, 0.f, 1.f));
+      const float4 a1 = make_float4(clampf(r1[c].x, 0.f, 1.f), clampf(r1[c].y, 0.f, 1.f),
+                                    clampf(r1[c].z, 0.f, 1.f), clampf(r1[c].w, 0.f, 1.f));
+      // imageStore(gid*3 + (dx,dy)): res0 -> (0,0),(0,1),(0,2),(1,0); centre (1,1);
+      // res1 -> (1,2),(2,0),(2,1),(2,2)   (compute/ravu-3x-r2.hook:106-114)
+      T* o = static_cast<T*>(p.out[c]);
+      const size_t op = p.out_pitch[c];
+      T* r = o + (size_t)(3 * gy) * op + 3 * gx;
+      stp(r, a0.x); stp(r + 1, a0.w); stp(r + 2, a1.y);
+      r += op;
+      stp(r, a0.y); stp(r + 1, v); stp(r + 2, a1.z);
+      r += op;
+      stp(r, a0.z); stp(r + 1, a1.x); stp(r + 2, a1.w);
+    }
+  }
+};
+
+// ------------------------------------------------------ ravu lattice -----
+// int11: the keyed filter over the input window.  Writes int11 and the input
+// copy straight into the output plane at (2i+1, 2j+1) and (2i, 2j).
+template <int R, int CM, typename T>
+struct Int11Tile {
+  static constexpr int N = 2 * R, S = N * N, HALO = R - 1;
+  static constexpr int TW = kTileW + N - 1, TH = kTileH + N - 1;
+  static constexpr int C = CM == kLuma ? 1 : 3;
+  static constexpr size_t smem_bytes = (size_t)(C + (CM == kRgb ? 1 : 0)) * TW * TH * 4;
+
+  __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem) {
+    float* tile = smem;
+    float* ltile = smem + C * TW * TH;
+    stage_planes<CM, TW, TH, T>(tile, ltile, p, x0 - HALO, y0 - HALO);
+    __syncthreads();
+    const int tx = threadIdx.x % kTileW, ty = threadIdx.x / kTileW;
+    const int gx = x0 + tx, gy = y0 + ty;
+    if (gx >= p.W || gy >= p.H) return;
+    auto val = [&](int c, int i) { return tile[c * TW * TH + (ty + i % N) * TW + tx + i / N]; };
+    auto lum = [&](int kx, int ky) {
+      return CM == kRgb ? ltile[(ty + ky) * TW + tx + kx] : tile[(ty + ky) * TW + tx + kx];
+    };
+    float a, b, d;
+    structure_tensor<N, true>(lum, p.kp, a, b, d);
+    const int key = ravu_key(a, b, d, p.kp);
+    if (p.keys) p.keys[(size_t)gy * p.W + gx] = key;
+    const float4* L = p.lut + (size_t)min(max(key, 0), p.lut_rows - 1) * p.lut_cols;
+    float res[C];
+#pragma unroll
+    for (int c = 0; c < C; c++) res[c] = 0.0f;
+#pragma unroll
+    for (int q = 0; q < (S / 2 + 3) / 4; q++) {
+      const float4 w4 = __ldg(L + q);
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const int i = 4 * q + j;
+        if (i < S / 2) {
+          const float w = j == 0 ? w4.x : (j == 1 ? w4.y : (j == 2 ? w4.z : w4.w));
+#pragma unroll
+          for (int c = 0; c < C; c++) res[c] += (val(c, i) + val(c, S - 1 - i)) * w;
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+      T* o = static_cast<T*>(p.out[c]);
+      const size_t op = p.out_pitch[c];
+      stp(o + (size_t)(2 * gy) * op + 2 * gx, tile[c * TW * TH + (ty + HALO) * TW + tx + HALO]);
+      stp(o + (size_t)(2 * gy + 1) * op + 2 * gx + 1, clampf(res[c], 0.f, 1.f));
+    }
+  }
+};
+
+// Where lattice sample k (grid (k/N, k%N)) of an int10 (L=0) or int01 (L=1)
+// pass reads: 0 = input, 1 = int11, at offsets (dx, dy).  The window is the
+// 45-degree lattice: s = kx+ky-(N-1), d = ky-kx (ravu-r3.hook:155-189 int10,
+// :289-323 int01).
+template <int N>
+__host__ __device__ constexpr int lat_src(int k, int L) {
+  return (((k / N + k % N - (N - 1)) % 2 != 0) == (L == 0)) ? 0 : 1;
+}
+template <int N>
+__host__ __device__ constexpr int lat_dx(int k, int L) {
+  // int10: input (s+1)/2, int11 s/2; int01: input s/2, int11 (s-1)/2
+  return L == 0 ? (lat_src<N>(k, L) == 0 ? (k / N + k % N - (N - 1) + 1) / 2 : (k / N + k % N - (N - 1)) / 2)
+                : (lat_src<N>(k, L) == 0 ? (k / N + k % N - (N - 1)) / 2 : (k / N + k % N - (N - 1) - 1) / 2);
+}
+template <int N>
+__host__ __device__ constexpr int lat_dy(int k, int L) {
+  // int10: input d/2, int11 (d-1)/2; int01: input (d+1)/2, int11 d/2
+  return L == 0 ? (lat_src<N>(k, L) == 0 ? (k % N - k / N) / 2 : (k % N - k / N - 1) / 2)
+                : (lat_src<N>(k, L) == 0 ? (k % N - k / N + 1) / 2 : (k % N - k / N) / 2);
+}
+
+// int10 + int01: both lattice filters per input pixel.  The int11 tile is
+// read back from the output plane at clamped int11 coordinates (the
+// clamp-to-edge of the int11 texture).
+template <int R, int CM, typename T>
+struct LatticeTile {
+  static constexpr int N = 2 * R, S = N * N;
+  static constexpr int TW = kTileW + N - 1, TH = kTileH + N - 1;
+  static constexpr int C = CM == kLuma ? 1 : 3;
+  static constexpr int PL = C + (CM == kRgb ? 1 : 0);  // planes per tile set
+  static constexpr size_t smem_bytes = (size_t)2 * PL * TW * TH * 4;
+
+  __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem) {
+    float* tin = smem;                      // input, offsets -(R-1) .. R
+    float* lin = tin + C * TW * TH;
+    float* t11 = smem + PL * TW * TH;       // int11, offsets -R .. R-1
+    float* l11 = t11 + C * TW * TH;
+    stage_planes<CM, TW, TH, T>(tin, lin, p, x0 - (R - 1), y0 - (R - 1));
+    for (int i = threadIdx.x; i < TW * TH; i += kTileThreads) {
+      const int ty = i / TW, tx = i % TW;
+      const int cx = clampi(x0 - R + tx, 0, p.W - 1), cy = clampi(y0 - R + ty, 0, p.H - 1);
+      float v[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+      for (int c = 0; c < C; c++) {
+        v[c] = ldp(static_cast<const T*>(p.out[c]) + (size_t)(2 * cy + 1) * p.out_pitch[c] + 2 * cx + 1);
+        t11[c * TW * TH + i] = v[c];
+      }
+      if (CM == kRgb) l11[i] = rgb_luma(v[0], v[1], v[2]);
+    }
+    __syncthreads();
+    const int tx = threadIdx.x % kTileW, ty = threadIdx.x / kTileW;
+    const int gx = x0 + tx, gy = y0 + ty;
+    if (gx >= p.W || gy >= p.H) return;
+#pragma unroll
+    for (int L = 0; L < 2; L++) {
+      auto idx = [&](int k) {
+        return lat_src<N>(k, L) == 0 ? (ty + lat_dy<N>(k, L) + R - 1) * TW + tx + lat_dx<N>(k, L) + R - 1
+                                     : (ty + lat_dy<N>(k, L) + R) * TW + tx + lat_dx<N>(k, L) + R;
+      };
+      auto val = [&](int c, int k) { return (lat_src<N>(k, L) == 0 ? tin : t11)[c * TW * TH + idx(k)]; };
+      auto lum = [&](int kx, int ky) {
+        const int k = kx * N + ky;
+        if (CM != kRgb) return val(0, k);
+        return (lat_src<N>(k, L) == 0 ? lin : l11)[idx(k)];
+      };
+      float a, b, d;
+      structure_tensor<N, true>(lum, p.kp, a, b, d);
+      const int key = ravu_key(a, b, d, p.kp);
+      if (p.keys) p.keys[(size_t)(1 + L) * p.W * p.H + (size_t)gy * p.W + gx] = key;
+      const float4* Lr = p.lut + (size_t)min(max(key, 0), p.lut_rows - 1) * p.lut_cols;
+      float res[C];
+#pragma unroll
+      for (int c = 0; c < C; c++) res[c] = 0.0f;
+#pragma unroll
+      for (int q = 0; q < (S / 2 + 3) / 4; q++) {
+        const float4 w4 = __ldg(Lr + q);
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const int i = 4 * q + j;
+          if (i < S / 2) {
+            const float w = j == 0 ? w4.x : (j == 1 ? w4.y : (j == 2 ? w4.z : w4.w));
+#pragma unroll
+            for (int c = 0; c < C; c++) res[c] += (val(c, i) + val(c, S - 1 - i)) * w;
+          }
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < C; c++) {
+        T* o = static_cast<T*>(p.out[c]);
+        const size_t op = p.out_pitch[c];
+        if (L == 0)
+          stp(o + (size_t)(2 * gy) * op + 2 * gx + 1, clampf(res[c], 0.f, 1.f));  // int10
+        else
+          stp(o + (size_t)(2 * gy + 1) * op + 2 * gx, clampf(res[c], 0.f, 1.f));  // int01
+      }
+    }
+  }
+};
+
+// ------------------------------------------------------------ ravu-zoom ---
+struct ZoomPos {
+  int i;    // floor(pos - 0.5)
+  float s;  // fract(pos - 0.5)
+};
+
+// pos - 0.5 = ((2X+1) W - OW) / (2 OW), taken exactly (centre-aligned map).
+__device__ __forceinline__ ZoomPos zoom_pos(int X, int W, int OW) {
+  const long long num = (2LL * X + 1) * W - OW;
+  const long long den = 2LL * OW;
+  const long long q = num >= 0 ? num / den : -((-num + den - 1) / den);
+  return {(int)q, (float)(num - q * den) / (float)den};
+}
+
+// Bilinear (FILTER LINEAR) fetch of one LUT texel at block column `blk` and
+// sub-position (sx, sy) of key block `key`: x = blk*9 + 8 sx, y = key*9 + 8 sy
+// (LUTPOS(x, 9) / (blocks, 288), ravu-zoom-r2.hook:23-31); clamp-to-edge.
+__device__ __forceinline__ float4 lut_bilinear(const float4* lut, int rows, int cols, int key, int blk, float sx,
+                                               float sy) {
+  const float fx8 = 8.0f * sx, fy8 = 8.0f * sy;
+  const float x0f = floorf(fx8), y0f = floorf(fy8);
+  const float fx = fx8 - x0f, fy = fy8 - y0f;
+  const int xa = min(blk * 9 + (int)x0f, cols - 1), xb = min(xa + 1, cols - 1);
+  const int ya = clampi(key * 9 + (int)y0f, 0, rows - 1), yb = min(ya + 1, rows - 1);
+  const float4 v00 = __ldg(lut + (size_t)ya * cols + xa), v01 = __ldg(lut + (size_t)ya * cols + xb);
+  const float4 v10 = __ldg(lut + (size_t)yb * cols + xa), v11 = __ldg(lut + (size_t)yb * cols + xb);
+  const float gx = 1.0f - fx, gy = 1.0f - fy;
+  float4 r;
+  r.x = (v00.x * gx + v01.x * fx) * gy + (v10.x * gx + v11.x * fx) * fy;
+  r.y = (v00.y * gx + v01.y * fx) * gy + (v10.y * gx + v11.y * fx) * fy;
+  r.z = (v00.z * gx + v01.z * fx) * gy + (v10.z * gx + v11.z * fx) * fy;
+  r.w = (v00.w * gx + v01.w * fx) * gy + (v10.w * gx + v11.w * fx) * fy;
+  return r;
+}
+
+__device__ __forceinline__ float comp4(const float4& v, int i) {
+  return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
+}
+
+// One thread per OUTPUT pixel; the tile is 32 x 8 output pixels and stages the
+// input rectangle they touch (at most (32+N+1) x (8+N+1) when upscaling).
+template <int R, int CM, bool AR, typename T>
+struct ZoomTile {
+  static constexpr int N = 2 * R, S = N * N, LO = R - 1;
+  static constexpr int RW = kTileW + N + 1, RH = kTileH + N + 1;
+  static constexpr int C = CM == kLuma ? 1 : 3;
+  static constexpr int NB = (S / 2 + 3) / 4;  // LUT texels per half window
+  static constexpr size_t smem_bytes = (size_t)(C + (CM == kRgb ? 1 : 0)) * RW * RH * 4;
+
+  __device__ static void run(const RavuArgs& p, int X0, int Y0, float* smem) {
+    float* tile = smem;
+    float* ltile = smem + C * RW * RH;
+    const int X1 = min(X0 + kTileW - 1, p.OW - 1), Y1 = min(Y0 + kTileH - 1, p.OH - 1);
+    const int rx = zoom_pos(X0, p.W, p.OW).i - LO, ry = zoom_pos(Y0, p.H, p.OH).i - LO;
+    const int rw = zoom_pos(X1, p.W, p.OW).i + R - rx + 1, rh = zoom_pos(Y1, p.H, p.OH).i + R - ry + 1;
+    if (rw > RW || rh > RH) {  // only reachable when downscaling, which the host rejects
+      if (threadIdx.x == 0 && p.err) atomicCAS(p.err, 0, kErrTileOverflow);
+      return;
+    }
+    for (int i = threadIdx.x; i < rw * rh; i += kTileThreads) {
+      const int ty = i / rw, tx = i % rw;
+      const int gx = clampi(rx + tx, 0, p.W - 1), gy = clampi(ry + ty, 0, p.H - 1);
+      float v[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+      for (int c = 0; c < C; c++) {
+        v[c] = ldp(static_cast<const T*>(p.in[c]) + (size_t)gy * p.in_pitch[c] + gx);
+        tile[c * RW * RH + ty * RW + tx] = v[c];
+      }
+      if (CM == kRgb) ltile[ty * RW + tx] = rgb_luma(v[0], v[1], v[2]);
+    }
+    __syncthreads();
+    const int X = X0 + threadIdx.x % kTileW, Y = Y0 + threadIdx.x / kTileW;
+    if (X >= p.OW || Y >= p.OH) return;
+    const ZoomPos px = zoom_pos(X, p.W, p.OW), py = zoom_pos(Y, p.H, p.OH);
+    const int bx = px.i - LO - rx, by = py.i - LO - ry;  // window origin in the tile
+    auto val = [&](int c, int k) { return tile[c * RW * RH + (by + k % N) * RW + bx + k / N]; };
+    auto lum = [&](int kx, int ky) {
+      return CM == kRgb ? ltile[(by + ky) * RW + bx + kx] : tile[(by + ky) * RW + bx + kx];
+    };
+    float a, b, d;
+    structure_tensor<N, true>(lum, p.kp, a, b, d);
+    const int key = ravu_key(a, b, d, p.kp);  // no +0.5 row centring (ravu-zoom-r2.hook:124)
+    if (p.keys) p.keys[(size_t)Y * p.OW + X] = key;
+    const float sx = px.s, sy = py.s, ix = 1.0f - sx, iy = 1.0f - sy;
+    float res[C], hi[C], lo[C], hi2[C], lo2[C];
+#pragma unroll
+    for (int c = 0; c < C; c++) res[c] = hi[c] = lo[c] = hi2[c] = lo2[c] = 0.0f;
+#pragma unroll
+    for (int blk = 0; blk < NB; blk++) {
+      const float4 ws = lut_bilinear(p.lut, p.lut_rows, p.lut_cols, key, blk, sx, sy);
+      const float4 wi = lut_bilinear(p.lut, p.lut_rows, p.lut_cols, key, blk, ix, iy);
+      float4 as = make_float4(0.f, 0.f, 0.f, 0.f), ai = as;
+      if (AR) {
+        as = lut_bilinear(p.lut_ar, p.lut_rows, p.lut_cols, key, blk, sx, sy);
+        ai = lut_bilinear(p.lut_ar, p.lut_rows, p.lut_cols, key, blk, ix, iy);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const int i = blk * 4 + j;
+        if (i < S / 2) {
+          const int k2 = S - 1 - i;
+#pragma unroll
+          for (int c = 0; c < C; c++) {
+            const float va = val(c, i), vb = val(c, k2);
+            res[c] += va * comp4(ws, j);
+            res[c] += vb * comp4(wi, j);
+            if (AR) {
+              const ArPow pa = ar_pow(va), pb = ar_pow(vb);
+              const float wa = comp4(as, j), wb = comp4(ai, j);
+              hi[c] += pa.h32 * wa + pb.h32 * wb;
+              lo[c] += pa.l32 * wa + pb.l32 * wb;
+              hi2[c] += pa.h33 * wa + pb.h33 * wb;
+              lo2[c] += pa.l33 * wa + pb.l33 * wb;
+            }
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+      const float v = AR ? ar_finish(res[c], lo[c], hi[c], lo2[c], hi2[c], p.ar) : clampf(res[c], 0.f, 1.f);
+      stp(static_cast<T*>(p.out[c]) + (size_t)Y * p.out_pitch[c] + X, v);
+    }
+  }
+};
+
+// One CTA per tile of a single frame.
+template <class Prog>
+__global__ void __launch_bounds__(kTileThreads) tile_kernel(const __grid_constant__ RavuArgs p) {
+  extern __shared__ float4 tile_smem[];
+  Prog::run(p, blockIdx.x * kTileW, blockIdx.y * kTileH, reinterpret_cast<float*>(tile_smem));
+}
+
+template <class Prog>
+int launch_tiles(const RavuArgs& a, int tiles_w, int tiles_h, cudaStream_t s) {
+  constexpr size_t smem = Prog::smem_bytes;
+  static_assert(smem <= 48 * 1024, "tile program needs more than the default shared memory");
+  tile_kernel<Prog><<<dim3(tiles_w, tiles_h), kTileThreads, smem, s>>>(a);
+  return 0;
+}
+
+}  // namespace pz

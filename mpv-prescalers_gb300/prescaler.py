@@ -248,6 +248,56 @@ class HookModel:
             self.run_raw(pl, res, out_size=(OW, OH), precision=precision, keys=keys, stream=stream)
         return self._pack(res, planes, as_list, keys, return_keys)
 
+    def upscale_host(self, frames, out=None, out_size: Optional[Tuple[int, int]] = None, precision: str = "fp32",
+                     device=None, depth: int = 3):
+        """Upscale host frames ``[N][C][H][W]`` (pinned CPU tensor) into host
+        memory, overlapping the copies with the kernels.
+
+        Frame i is copied to the device on a copy stream, upscaled on a
+        compute stream and copied back on a third stream, so the transfers
+        of neighbouring frames run under frame i's kernels.  ``depth`` device
+        buffers rotate (3: one in flight on each stream).  Returns the host
+        output ``[N][C][OH][OW]`` (``out`` if given; it should be pinned).
+        """
+        torch = _torch()
+        if frames.dim() != 4 or frames.is_cuda:
+            raise ValueError("frames must be a host tensor [N][C][H][W]")
+        dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        N, C, H, W = frames.shape
+        OW, OH = self.output_size(W, H, out_size)
+        if out is None:
+            out = torch.empty((N, C, OH, OW), dtype=frames.dtype, pin_memory=True)
+        with torch.cuda.device(dev):
+            s_in, s_run, s_out = torch.cuda.Stream(dev), torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+            xin = [torch.empty((C, H, W), dtype=frames.dtype, device=dev) for _ in range(depth)]
+            yout = [torch.empty((C, OH, OW), dtype=frames.dtype, device=dev) for _ in range(depth)]
+            copied = [torch.cuda.Event() for _ in range(depth)]
+            done = [torch.cuda.Event() for _ in range(depth)]
+            drained = [None] * depth
+            for i in range(N):
+                b = i % depth
+                if drained[b] is not None:       # buffer b's previous frame has left
+                    s_in.wait_event(drained[b])
+                with torch.cuda.stream(s_in):
+                    xin[b].copy_(frames[i], non_blocking=True)
+                    copied[b].record(s_in)
+                s_run.wait_event(copied[b])
+                if drained[b] is not None:
+                    s_run.wait_event(drained[b])
+                self.run_raw(list(xin[b].unbind(0)), list(yout[b].unbind(0)), out_size=(OW, OH),
+                             precision=precision, stream=s_run)
+                done[b].record(s_run)
+                s_out.wait_event(done[b])
+                with torch.cuda.stream(s_out):
+                    out[i].copy_(yout[b], non_blocking=True)
+                    ev = torch.cuda.Event()
+                    ev.record(s_out)
+                    drained[b] = ev
+            s_out.synchronize()
+            for t in xin + yout:   # buffers were used on side streams
+                t.record_stream(s_out)
+        return out
+
     def key_shape(self, W, H, OW, OH):
         fam = self.family
         if fam == "ravu":

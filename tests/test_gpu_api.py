@@ -1,0 +1,47 @@
+"""Public API behaviour on the GPU: batches, host pipelines, //!WHEN."""
+import numpy as np
+import pytest
+
+from mpv_prescalers_gb300 import synth
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.fail("CUDA device required for -m gpu tests")
+    yield
+
+
+@pytest.mark.parametrize("name", ["ravu-lite-ar-r3", "ravu-r3-yuv", "nnedi3-nns32-win8x4"])
+def test_host_pipeline_matches_device_calls(name):
+    hm, _ = synth.model_for(name)
+    C = hm.n_planes
+    frames = torch.stack([torch.from_numpy(synth.frame(36, 52, 100 + i, hm.channels)) for i in range(5)])
+    frames = frames.to(torch.float16).pin_memory()
+    got = hm.upscale_host(frames)
+    assert got.shape == (5, C, 72, 104)
+    for i in range(5):
+        ref = hm.upscale(frames[i].cuda()).cpu()
+        assert torch.equal(got[i], ref)
+
+
+def test_batch_of_frames_matches_frame_by_frame():
+    hm, _ = synth.model_for("ravu-zoom-ar-r2-rgb")
+    x = torch.stack([torch.from_numpy(synth.rgb_frame(30, 40, 7 + i)) for i in range(3)]).cuda()
+    y = hm.upscale(x, out_size=(70, 51))
+    assert y.shape == (3, 3, 51, 70)
+    for i in range(3):
+        assert torch.equal(y[i], hm.upscale(x[i], out_size=(70, 51)))
+
+
+def test_when_false_leaves_planes_untouched():
+    hm, _ = synth.model_for("ravu-lite-r3")
+    x = torch.rand((40, 60), device="cuda")
+    y = hm.upscale(x, out_size=(70, 50))  # 0.86x per axis: //!WHEN wants < 0.707
+    assert torch.equal(y, x)
+    nn, _ = synth.model_for("nnedi3-nns16-win8x4")
+    y = nn.upscale(x, out_size=(60, 80))  # rows only
+    assert y.shape == (80, 60)
