@@ -272,6 +272,23 @@ def run_gpu(args):
                        "ratio": res["fast"] / res["fp32"], "chosen": "FP16 planes" + (
                            ", FP16 tensor-core neurons" if n.startswith("nnedi3") else ", FP32 math")}
 
+    # ---- serving: Poisson arrivals over 64 streams, mixed resolutions and
+    # algorithms (the serving configuration), against serial plain FP32
+    serving = None
+    if args.serve_requests > 0:
+        from mpv_prescalers_gb300 import serve
+        smodels = {name: synth.model_for(name)[0] for name, _ in serve.ALGORITHMS}
+        trace = serve.poisson_trace(smodels, args.serve_requests, rate=240.0, streams=64, frame_pool=1)
+        warm = serve.poisson_trace(smodels, 16, rate=2000.0, streams=64, frame_pool=1)
+        serve.Server(smodels).run(warm)
+        srv = serve.Server(smodels, hbm_budget=40e9, slots=8)
+        served = srv.run(trace)
+        serial = serve.serial_baseline(smodels, trace)
+        serving = {"trace": f"{len(trace)} requests, Poisson 240 frames/s over 64 streams, resolutions "
+                            "{480p .3, 720p .3, 1080p .3, 2160p .1}, algorithms {ravu-lite-ar-r3, ravu-r4-yuv, "
+                            "nnedi3-nns64-win8x4, ravu-zoom-ar-r2 at 1.75x}, FP16 planes, 40 GB budget",
+                   "served": served, "serial_fp32": serial}
+
     props = torch.cuda.get_device_properties(dev)
     clocks = clk.summary()
     sm_mhz = clocks["sm_mhz"] or 0.0
@@ -312,6 +329,7 @@ def run_gpu(args):
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clocks,
         "headline": headline,
+        "serving": serving,
         "device": props.name,
     }
     if world > 1:
@@ -357,6 +375,7 @@ def main():
     ap.add_argument("--cpu-rows", type=int, default=1080, help="input rows per model in the CPU sample")
     ap.add_argument("--ref-rows", type=int, default=540)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=480, help="requests in the serving trace (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3

@@ -1,0 +1,249 @@
+"""Serving loop: continuous batching of prescaler requests from many streams.
+
+A request is one host frame of one video stream through one model (the
+frames a player's render loop would hand to the hook chain).  The server
+
+* keeps every model's LUT / weights resident on the device;
+* admits queued requests in arrival order while the device-memory they need
+  (input + output planes + NNEDI3 scratch) fits the HBM budget and an
+  execution slot is free -- requests arriving while others run are admitted
+  as soon as memory and slots free up;
+* runs each admitted request on its slot's CUDA stream (host->device copy,
+  the model's kernels, device->host copy), so the work of different
+  requests overlaps on the device; in ``mode="batch"`` the requests admitted
+  together are launched as one persistent batch (``batch.Batch``);
+* records per-request latency from arrival to the moment the output is back
+  in host memory (CUDA event time), and reports p50/p99, throughput and the
+  peak device memory in use.
+
+``serial_baseline`` runs the same trace one request at a time in plain FP32
+planes with no overlap, the comparison point for the served numbers.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import batch as _batch
+from .prescaler import HookModel
+
+
+def _torch():
+    import torch
+    return torch
+
+
+@dataclass
+class Request:
+    rid: int
+    stream_id: int
+    model: str
+    frame: "torch.Tensor"                 # host [C][H][W] (pinned)
+    arrival: float                        # seconds from trace start
+    out_size: Optional[Tuple[int, int]] = None
+    precision: str = "fast"
+    # filled in by the server
+    admit: float = -1.0
+    finish: float = -1.0
+    output: Optional["torch.Tensor"] = None
+
+    @property
+    def latency(self) -> float:
+        return self.finish - self.arrival
+
+
+def request_bytes(model: HookModel, frame, out_size) -> int:
+    """Device bytes one request holds while in flight."""
+    C, H, W = frame.shape
+    OW, OH = model.output_size(W, H, out_size)
+    es = frame.element_size()
+    nbytes = C * (H * W + OH * OW) * es
+    if model.family == "nnedi3" and model.nnedi3_axes(W, H, (OW, OH)) == 3:
+        nbytes += 2 * H * W * es
+    return nbytes
+
+
+@dataclass
+class _Slot:
+    stream: "torch.cuda.Stream"
+    reqs: List[Request] = field(default_factory=list)
+    done: Optional["torch.cuda.Event"] = None
+    nbytes: int = 0
+    keep: list = field(default_factory=list)   # device tensors of the in-flight requests
+
+
+class Server:
+    def __init__(self, models: Dict[str, HookModel], hbm_budget: float = 40e9, slots: int = 8,
+                 mode: str = "streams", device: Optional[int] = None):
+        torch = _torch()
+        if mode not in ("streams", "batch"):
+            raise ValueError(mode)
+        self.models = models
+        self.budget = int(hbm_budget)
+        self.mode = mode
+        self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        self.slots = [_Slot(torch.cuda.Stream(self.device)) for _ in range(slots)]
+        for m in models.values():       # weights / LUTs resident before the first request
+            m.device_handle(self.device.index)
+        self.in_use = 0
+        self.peak = 0
+        self.rejected: List[Request] = []
+
+    # -- one admitted group on one slot ------------------------------------
+    def _launch(self, slot: _Slot, reqs: List[Request], now: float):
+        torch = _torch()
+        jobs = []
+        with torch.cuda.stream(slot.stream):
+            for r in reqs:
+                m = self.models[r.model]
+                xd = r.frame.to(self.device, non_blocking=True)
+                job = _batch.Job.make(m, xd, out_size=r.out_size, precision=r.precision)
+                jobs.append(job)
+                slot.keep += [xd] + job.outputs + ([job.scratch] if job.scratch is not None else [])
+            if self.mode == "batch" and len(jobs) > 1:
+                b = _batch.Batch(jobs, stream=slot.stream)
+                b.launch(stream=slot.stream)
+                slot.keep.append(b)
+            else:
+                _batch.run_per_job(jobs, stream=slot.stream)
+            for r, job in zip(reqs, jobs):
+                out = torch.stack(job.outputs)
+                r.output = torch.empty(out.shape, dtype=out.dtype, pin_memory=True)
+                r.output.copy_(out, non_blocking=True)
+                slot.keep.append(out)
+            slot.done = torch.cuda.Event(enable_timing=True)
+            slot.done.record(slot.stream)
+        for r in reqs:
+            r.admit = now
+        slot.reqs = reqs
+
+    def run(self, trace: Sequence[Request], max_group: int = 4) -> Dict[str, float]:
+        """Serve a trace in real time; returns latency / throughput stats."""
+        torch = _torch()
+        pending = sorted(trace, key=lambda r: r.arrival)
+        queue: List[Request] = []
+        t0_event = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(self.device)
+        t0_event.record(torch.cuda.current_stream(self.device))
+        t0 = time.perf_counter()
+        i = 0
+        done: List[Request] = []
+        while i < len(pending) or queue or any(s.reqs for s in self.slots):
+            now = time.perf_counter() - t0
+            while i < len(pending) and pending[i].arrival <= now:
+                queue.append(pending[i])
+                i += 1
+            # retire finished slots
+            for s in self.slots:
+                if s.reqs and s.done.query():
+                    fin = t0_event.elapsed_time(s.done) / 1e3
+                    for r in s.reqs:
+                        r.finish = fin
+                        done.append(r)
+                    self.in_use -= s.nbytes
+                    s.reqs, s.keep, s.nbytes, s.done = [], [], 0, None
+            # admit in arrival order while memory and slots allow
+            for s in self.slots:
+                if s.reqs or not queue:
+                    continue
+                group, nbytes = [], 0
+                while queue and len(group) < max_group:
+                    r = queue[0]
+                    need = request_bytes(self.models[r.model], r.frame, r.out_size)
+                    if need > self.budget:  # can never fit: refuse it rather than stall the queue
+                        self.rejected.append(queue.pop(0))
+                        continue
+                    if self.in_use + nbytes + need > self.budget:
+                        break
+                    group.append(queue.pop(0))
+                    nbytes += need
+                    if self.mode == "streams":
+                        break
+                if not group:
+                    break
+                self.in_use += nbytes
+                self.peak = max(self.peak, self.in_use)
+                s.nbytes = nbytes
+                self._launch(s, group, now)
+            if i < len(pending) and not queue and not any(s.reqs for s in self.slots):
+                time.sleep(max(0.0, min(pending[i].arrival - (time.perf_counter() - t0), 0.002)))
+            else:
+                time.sleep(2e-5)
+        return summarize(done, self.peak)
+
+
+def summarize(done: Sequence[Request], peak_bytes: int = 0) -> Dict[str, float]:
+    lat = np.array([r.latency for r in done]) * 1e3
+    span = max(r.finish for r in done) - min(r.arrival for r in done)
+    px = sum(r.output.shape[-1] * r.output.shape[-2] for r in done)
+    return {"requests": len(done), "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean()), "max_ms": float(lat.max()), "out_mpix_s": px / span / 1e6,
+            "span_s": span, "peak_hbm_gb": peak_bytes / 1e9}
+
+
+def serial_baseline(models: Dict[str, HookModel], trace: Sequence[Request]) -> Dict[str, float]:
+    """The same trace, one request at a time, FP32 planes, no overlap: each
+    request starts when it has arrived and the previous one has finished."""
+    torch = _torch()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    clock = 0.0
+    done = []
+    for r in sorted(trace, key=lambda q: q.arrival):
+        q = Request(r.rid, r.stream_id, r.model, r.frame.float(), r.arrival, r.out_size, "fp32")
+        start = max(clock, q.arrival)
+        torch.cuda.synchronize(dev)
+        t = time.perf_counter()
+        xd = q.frame.to(dev)
+        y = models[q.model].upscale(xd, out_size=q.out_size, precision="fp32")
+        q.output = y.cpu()
+        torch.cuda.synchronize(dev)
+        clock = start + (time.perf_counter() - t)
+        q.finish = clock
+        done.append(q)
+    return summarize(done)
+
+
+# ------------------------------------------------------------------ traces --
+
+RESOLUTIONS = ((854, 480, 0.3), (1280, 720, 0.3), (1920, 1080, 0.3), (3840, 2160, 0.1))
+ALGORITHMS = (("ravu-lite-ar-r3", None), ("ravu-r4-yuv", None), ("nnedi3-nns64-win8x4", None),
+              ("ravu-zoom-ar-r2", 1.75))
+
+
+def poisson_trace(models: Dict[str, HookModel], n: int, rate: float = 240.0, streams: int = 64,
+                  seed: int = 5000, precision: str = "fast", frame_pool: int = 2,
+                  resolutions=RESOLUTIONS, algorithms=ALGORITHMS) -> List[Request]:
+    """Poisson arrivals at `rate` frames/s over `streams` streams; resolution
+    and algorithm drawn per stream (the mix of the serving configuration).
+    Frames come from a small pool of seeded synthetic frames per resolution."""
+    from . import synth
+    torch = _torch()
+    rng = np.random.default_rng(seed)
+    res_p = np.array([r[2] for r in resolutions])
+    stream_res = rng.choice(len(resolutions), size=streams, p=res_p / res_p.sum())
+    stream_alg = rng.integers(0, len(algorithms), size=streams)
+    pool: Dict[Tuple[int, str], List] = {}
+
+    def frame(ri: int, channels: str, k: int):
+        key = (ri, channels)
+        if key not in pool:
+            W, H, _ = resolutions[ri]
+            pool[key] = [torch.from_numpy(synth.frame(H, W, seed + 17 * ri + j, channels)).to(torch.float16)
+                         .pin_memory() for j in range(frame_pool)]
+        return pool[key][k % frame_pool]
+
+    t = 0.0
+    out = []
+    for rid in range(n):
+        t += rng.exponential(1.0 / rate)
+        sid = int(rng.integers(0, streams))
+        name, zoom = algorithms[stream_alg[sid]]
+        W, H, _ = resolutions[stream_res[sid]]
+        m = models[name]
+        f = frame(int(stream_res[sid]), m.channels, rid)
+        osz = (int(round(W * zoom)), int(round(H * zoom))) if zoom else None
+        out.append(Request(rid, sid, name, f, t, osz, precision))
+    return out
