@@ -50,7 +50,7 @@ class Job:
         H, W = pl[0].shape
         OW, OH = model.output_size(W, H, out_size)
         if out is None:
-            outs = [torch.empty((OH, OW), dtype=pl[0].dtype, device=pl[0].device) for _ in pl]
+            outs = list(torch.empty((len(pl), OH, OW), dtype=pl[0].dtype, device=pl[0].device).unbind(0))
         else:
             outs = [out] if out.dim() == 2 else list(out.unbind(0))
         scratch = None

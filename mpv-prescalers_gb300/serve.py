@@ -110,10 +110,10 @@ class Server:
             else:
                 _batch.run_per_job(jobs, stream=slot.stream)
             for r, job in zip(reqs, jobs):
-                out = torch.stack(job.outputs)
+                o0 = job.outputs[0]
+                out = o0.as_strided((len(job.outputs),) + tuple(o0.shape), (o0.numel(),) + tuple(o0.stride()))
                 r.output = torch.empty(out.shape, dtype=out.dtype, pin_memory=True)
                 r.output.copy_(out, non_blocking=True)
-                slot.keep.append(out)
             slot.done = torch.cuda.Event(enable_timing=True)
             slot.done.record(slot.stream)
         for r in reqs:
@@ -211,6 +211,27 @@ def serial_baseline(models: Dict[str, HookModel], trace: Sequence[Request]) -> D
 RESOLUTIONS = ((854, 480, 0.3), (1280, 720, 0.3), (1920, 1080, 0.3), (3840, 2160, 0.1))
 ALGORITHMS = (("ravu-lite-ar-r3", None), ("ravu-r4-yuv", None), ("nnedi3-nns64-win8x4", None),
               ("ravu-zoom-ar-r2", 1.75))
+
+
+def warmup_trace(models: Dict[str, HookModel], resolutions=RESOLUTIONS, algorithms=ALGORITHMS,
+                 precision: str = "fast") -> List[Request]:
+    """One request of every (resolution, algorithm) pair, back to back, so that
+    every kernel is loaded and the pinned host buffers of every output size
+    are cached before a measured trace."""
+    reqs = poisson_trace(models, 1, resolutions=resolutions, algorithms=algorithms, precision=precision,
+                         frame_pool=1)
+    from . import synth
+    torch = _torch()
+    out, rid = [], 0
+    for W, H, _ in resolutions:
+        for name, zoom in algorithms:
+            m = models[name]
+            f = torch.zeros((m.n_planes, H, W), dtype=torch.float16).pin_memory()
+            osz = (int(round(W * zoom)), int(round(H * zoom))) if zoom else None
+            out.append(Request(rid, 0, name, f, 0.0, osz, precision))
+            rid += 1
+    del reqs, synth
+    return out
 
 
 def poisson_trace(models: Dict[str, HookModel], n: int, rate: float = 240.0, streams: int = 64,
