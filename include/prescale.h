@@ -114,6 +114,9 @@ typedef struct {
                               key of every key evaluation (parity tests)     */
   void* scratch;           /* optional caller scratch for multi-pass chains  */
   size_t scratch_bytes;
+  int staging;             /* RAVU halo staging: 0 clamped loads, 1 TMA boxes
+                              for interior tiles (border tiles always use
+                              clamped loads: TMA fills zeros, not the edge)  */
 } pz_opts;
 
 int pz_version(void);

@@ -192,6 +192,28 @@ class PlanCache:
                 pass  # a read-only cache location only loses persistence
 
 
+def autotune_staging(model: HookModel, frame, out_size=None, precision: str = "fp32",
+                     cache: Optional[PlanCache] = None, reps: int = 5) -> Tuple[str, Dict[str, float]]:
+    """Time clamped-load vs TMA halo staging for one model and frame shape
+    on this GPU; the winner is cached per (GPU, model, shape, dtype)."""
+    torch = _torch()
+    cache = cache or PlanCache()
+    gpu = torch.cuda.get_device_name(frame.device)
+    key = f"{gpu}:staging:{model.name}:{tuple(frame.shape)}:{frame.dtype}:{out_size}:{precision}"
+    hit = cache.get(key)
+    if hit:
+        return hit["staging"], hit.get("times_ms", {})
+    pl = [frame] if frame.dim() == 2 else list(frame.unbind(0))
+    H, W = pl[0].shape
+    OW, OH = model.output_size(W, H, out_size)
+    outs = [torch.empty((OH, OW), dtype=frame.dtype, device=frame.device) for _ in pl]
+    times = {st: _time_ms(lambda st=st: model.run_raw(pl, outs, (OW, OH), precision=precision, staging=st), reps)
+             for st in ("ldg", "tma")}
+    best = min(times, key=times.get)
+    cache.put(key, {"staging": best, "times_ms": times})
+    return best, times
+
+
 def _time_ms(fn, reps: int) -> float:
     torch = _torch()
     fn()

@@ -1,5 +1,7 @@
 // C ABI of libprescale.so (declared in include/prescale.h): model upload,
 // argument checking, dispatch to the kernels, thread-local error messages.
+#include <cuda.h>
+
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -63,6 +65,39 @@ int check_plane(const pz_plane& p, const char* what, int idx, bool pairs) {
 }  // namespace
 
 namespace pz {
+// Tensor map of one plane for 2-D TMA boxes of box_w x box_h texels.  False
+// when the plane cannot be described (base or row pitch not 16-byte aligned,
+// plane smaller than a box, driver entry point missing): callers then use
+// clamped loads.
+bool encode_plane_map(CUtensorMap* map, const void* base, int W, int H, int pitch, int dtype, int box_w,
+                      int box_h) {
+  typedef CUresult (*EncodeFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                               const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                               CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  static EncodeFn encode = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      encode = reinterpret_cast<EncodeFn>(fn);
+  });
+  const size_t es = dtype == PZ_F32 ? 4 : 2;
+  if (!encode || W < box_w || H < box_h || box_w > 256 || box_h > 256) return false;
+  if (reinterpret_cast<uintptr_t>(base) % 16 || ((size_t)pitch * es) % 16) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)W, (cuuint64_t)H};
+  const cuuint64_t strides[1] = {(cuuint64_t)pitch * es};
+  const cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = encode(map, dtype == PZ_F32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16,
+                            2, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
 int set_error(int code, const char* fmt, ...) {
   char buf[512];
   va_list ap;
@@ -347,6 +382,7 @@ int pz_run(const pz_model* m, const pz_plane* in, int n_in, pz_plane* out, int n
     a.ar = m->ar;
     a.keys = o ? o->keys : nullptr;
     a.err = pz::device_error_word();
+    a.staging = o ? o->staging : 0;
     a.kp = m->kp;
     switch (m->family) {
       case PZ_RAVU_LITE: rc = pz::launch_lite(a, m->radius, m->ar != 0.0f, dt, s); break;

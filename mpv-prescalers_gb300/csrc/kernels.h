@@ -24,6 +24,7 @@ struct RavuArgs {
   float ar;
   int32_t* keys;     // optional raw-key output
   int* err;          // device error word (kErr*)
+  int staging;       // 0: clamped loads, 1: TMA boxes for interior tiles
   KeyParams kp;
 };
 

@@ -21,23 +21,13 @@
 //      e = exp(s1), s2 likewise, wsum += e, vsum += e * s2 / (1 + |s2|).
 // The mean term restores <x, A_k> * invstd exactly (x_hat is centred).
 // The CTA is persistent: weights and TMEM are set up once per CTA.
+#include "async.cuh"
 #include "kernels.h"
 
 namespace pz {
 namespace {
 
 constexpr int kThreads = 128;  // 4 warps, one TMEM lane quarter each
-constexpr unsigned long long kWaitNs = 1000000000ull;  // 1 s bound on every wait
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ unsigned long long globaltimer() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
 
 // tcgen05 shared-memory matrix descriptor, no swizzle, K-major.
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
@@ -65,28 +55,6 @@ __device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t a, uint64_t b,
 __device__ __forceinline__ void mma_commit(uint32_t mbar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
                : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}\n"
-      : "=r"(ok)
-      : "r"(mbar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Wait for phase `parity` of the mbarrier, giving up after kWaitNs.
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity) {
-  if (mbar_try(mbar, parity)) return true;
-  const unsigned long long t0 = globaltimer();
-  while (!mbar_try(mbar, parity)) {
-    if (globaltimer() - t0 > kWaitNs) return false;
-  }
-  return true;
 }
 
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
@@ -158,8 +126,7 @@ __global__ void __launch_bounds__(kThreads) nn_tc_kernel(const __grid_constant__
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    mbar_init(smem_u32(&mbar), 1);
     abort_flag = 0;
   }
   fence_async_smem();

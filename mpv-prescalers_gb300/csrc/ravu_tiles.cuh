@@ -17,6 +17,9 @@
 // t handles column t % 32 of row t / 32.  Out-of-range reads replicate the
 // edge texel (the mpv texture border mode).
 #pragma once
+#include <cstring>
+
+#include "async.cuh"
 #include "kernels.h"
 
 namespace pz {
@@ -53,6 +56,76 @@ __device__ __forceinline__ void stage_planes(float* tile, float* ltile, const Ra
   }
 }
 
+// ---------------------------------------------------------- TMA staging ---
+// Interior tiles (window fully inside the plane) can be staged by TMA: one
+// 2-D box per plane lands in shared memory, then one pass converts it to the
+// float tile the programs read.  Border tiles keep the clamped loads above,
+// because TMA fills out-of-range texels with zeros, not the edge value.  The
+// box starts at the tile origin rounded down to 8 columns, so its x
+// coordinate is 16-byte aligned for FP32 and FP16 planes.
+struct TmaMaps {
+  CUtensorMap map[3];
+};
+
+struct TmaCtx {
+  const CUtensorMap* map;  // one per plane, in kernel parameter space
+  uint32_t mbar;           // shared mbarrier (count 1), used once
+  unsigned char* raw;      // landing area, 128-byte aligned
+};
+
+template <int TW>
+__host__ __device__ constexpr int tma_box_w() {
+  return (TW + 7 + 7) & ~7;  // up to 7 lead columns from rounding the start down
+}
+template <int TW, int TH, typename T>
+__host__ __device__ constexpr uint32_t tma_plane_bytes() {
+  return ((uint32_t)tma_box_w<TW>() * TH * sizeof(T) + 127u) & ~127u;
+}
+
+__device__ __forceinline__ float lds_f(const float* p) { return *p; }
+__device__ __forceinline__ float lds_f(const __half* p) { return __half2float(*p); }
+
+// 1: staged by TMA; 0: not an interior tile (use clamped loads); -1: the
+// copy did not complete within the wait bound (error word set).
+template <int CM, int TW, int TH, typename T>
+__device__ int stage_planes_tma(const RavuArgs& p, const TmaCtx* t, int x0, int y0, float* tile, float* ltile) {
+  constexpr int C = CM == kLuma ? 1 : 3;
+  constexpr int BW = tma_box_w<TW>();
+  constexpr uint32_t PB = tma_plane_bytes<TW, TH, T>();
+  if (!t || x0 < 0 || y0 < 0 || x0 + TW > p.W || y0 + TH > p.H) return 0;
+  const int bx = x0 & ~7, off = x0 - bx;
+  if (threadIdx.x == 0) {
+    mbar_arrive_expect_tx(t->mbar, (uint32_t)C * BW * TH * sizeof(T));
+#pragma unroll
+    for (int c = 0; c < C; c++) tma_load_2d(t->raw + c * PB, &t->map[c], bx, y0, t->mbar);
+  }
+  if (!mbar_wait_bounded(t->mbar, 0)) {
+    if (threadIdx.x == 0 && p.err) atomicCAS(p.err, 0, kErrWaitTimeout);
+    return -1;
+  }
+  for (int i = threadIdx.x; i < TW * TH; i += kTileThreads) {
+    const int ty = i / TW, tx = i % TW;
+    float v[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+      v[c] = lds_f(reinterpret_cast<const T*>(t->raw + c * PB) + ty * BW + tx + off);
+      tile[c * TW * TH + i] = v[c];
+    }
+    if (CM == kRgb) ltile[i] = rgb_luma(v[0], v[1], v[2]);
+  }
+  return 1;
+}
+
+// Stage the frame tile by TMA when possible, else by clamped loads.
+// Returns false only when a TMA wait timed out (the tile is abandoned).
+template <int CM, int TW, int TH, typename T>
+__device__ __forceinline__ bool stage_frame(const RavuArgs& p, const TmaCtx* t, int x0, int y0, float* tile,
+                                            float* ltile) {
+  const int r = stage_planes_tma<CM, TW, TH, T>(p, t, x0, y0, tile, ltile);
+  if (r == 0) stage_planes<CM, TW, TH, T>(tile, ltile, p, x0, y0);
+  return r >= 0;
+}
+
 // ------------------------------------------------------------ ravu-lite ---
 // Does lite LUT column c take part in the anti-ringing sums?  r2: every
 // tap; r3/r4: the 13-tap diamond |dx|+|dy| <= 2 (ravu-lite-ar-r3.hook:93-170).
@@ -68,10 +141,13 @@ struct LiteTile {
   // value tile, then (AR) the anti-ringing powers of every tile value
   static constexpr size_t smem_bytes = (size_t)((TW * TH + 3) & ~3) * 4 + (AR ? (size_t)TW * TH * 16 : 0);
 
-  __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem) {
+  static constexpr int kPlanes = 1;
+  using Elem = T;
+
+  __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, const TmaCtx* tma = nullptr) {
     float* tile = smem;
     float4* ptile = reinterpret_cast<float4*>(smem + ((TW * TH + 3) & ~3));
-    stage_tile<TW, TH>(tile, static_cast<const T*>(p.in[0]), p.in_pitch[0], p.W, p.H, x0 - HALO, y0 - HALO);
+    if (!stage_frame<kLuma, TW, TH, T>(p, tma, x0 - HALO, y0 - HALO, tile, nullptr)) return;
     __syncthreads();
     if (AR) {  // (h32, l32, h33, l33) once per value instead of once per window tap
       for (int i = threadIdx.x; i < TW * TH; i += kTileThreads) {
@@ -155,11 +231,13 @@ struct ThreeXTile {
   static constexpr int TW = kTileW + N - 1, TH = kTileH + N - 1;
   static constexpr int C = CM == kLuma ? 1 : 3;
   static constexpr size_t smem_bytes = (size_t)(C + (CM == kRgb ? 1 : 0)) * TW * TH * 4;
+  static constexpr int kPlanes = C;
+  using Elem = T;
 
-  __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem) {
+  __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, const TmaCtx* tma = nullptr) {
     float* tile = smem;
     float* ltile = smem + C * TW * TH;
-    stage_planes<CM, TW, TH, T>(tile, ltile, p, x0 - HALO, y0 - HALO);
+    if (!stage_frame<CM, TW, TH, T>(p, tma, x0 - HALO, y0 - HALO, tile, ltile)) return;
     __syncthreads();
     const int tx = threadIdx.x % kTileW, ty = threadIdx.x / kTileW;
     const int gx = x0 + tx, gy = y0 + ty;
@@ -226,11 +304,13 @@ struct Int11Tile {
   static constexpr int TW = kTileW + N - 1, TH = kTileH + N - 1;
   static constexpr int C = CM == kLuma ? 1 : 3;
   static constexpr size_t smem_bytes = (size_t)(C + (CM == kRgb ? 1 : 0)) * TW * TH * 4;
+  static constexpr int kPlanes = C;
+  using Elem = T;
 
-  __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem) {
+  __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, const TmaCtx* tma = nullptr) {
     float* tile = smem;
     float* ltile = smem + C * TW * TH;
-    stage_planes<CM, TW, TH, T>(tile, ltile, p, x0 - HALO, y0 - HALO);
+    if (!stage_frame<CM, TW, TH, T>(p, tma, x0 - HALO, y0 - HALO, tile, ltile)) return;
     __syncthreads();
     const int tx = threadIdx.x % kTileW, ty = threadIdx.x / kTileW;
     const int gx = x0 + tx, gy = y0 + ty;
@@ -301,13 +381,15 @@ struct LatticeTile {
   static constexpr int C = CM == kLuma ? 1 : 3;
   static constexpr int PL = C + (CM == kRgb ? 1 : 0);  // planes per tile set
   static constexpr size_t smem_bytes = (size_t)2 * PL * TW * TH * 4;
+  static constexpr int kPlanes = C;
+  using Elem = T;
 
-  __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem) {
+  __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, const TmaCtx* tma = nullptr) {
     float* tin = smem;                      // input, offsets -(R-1) .. R
     float* lin = tin + C * TW * TH;
     float* t11 = smem + PL * TW * TH;       // int11, offsets -R .. R-1
     float* l11 = t11 + C * TW * TH;
-    stage_planes<CM, TW, TH, T>(tin, lin, p, x0 - (R - 1), y0 - (R - 1));
+    if (!stage_frame<CM, TW, TH, T>(p, tma, x0 - (R - 1), y0 - (R - 1), tin, lin)) return;
     for (int i = threadIdx.x; i < TW * TH; i += kTileThreads) {
       const int ty = i / TW, tx = i % TW;
       const int cx = clampi(x0 - R + tx, 0, p.W - 1), cy = clampi(y0 - R + ty, 0, p.H - 1);
@@ -418,7 +500,10 @@ struct ZoomTile {
   static constexpr int NB = (S / 2 + 3) / 4;  // LUT texels per half window
   static constexpr size_t smem_bytes = (size_t)(C + (CM == kRgb ? 1 : 0)) * RW * RH * 4;
 
-  __device__ static void run(const RavuArgs& p, int X0, int Y0, float* smem) {
+  static constexpr int kPlanes = 0;  // the input rectangle moves with the ratio: clamped loads only
+  using Elem = T;
+
+  __device__ static void run(const RavuArgs& p, int X0, int Y0, float* smem, const TmaCtx* = nullptr) {
     float* tile = smem;
     float* ltile = smem + C * RW * RH;
     const int X1 = min(X0 + kTileW - 1, p.OW - 1), Y1 = min(Y0 + kTileH - 1, p.OH - 1);
@@ -495,18 +580,50 @@ struct ZoomTile {
   }
 };
 
-// One CTA per tile of a single frame.
-template <class Prog>
-__global__ void __launch_bounds__(kTileThreads) tile_kernel(const __grid_constant__ RavuArgs p) {
-  extern __shared__ float4 tile_smem[];
-  Prog::run(p, blockIdx.x * kTileW, blockIdx.y * kTileH, reinterpret_cast<float*>(tile_smem));
+// One CTA per tile of a single frame; with TMA the frame tile of interior
+// tiles comes in by cp.async.bulk.tensor.
+template <class Prog, bool TMA>
+__global__ void __launch_bounds__(kTileThreads) tile_kernel(const __grid_constant__ RavuArgs p,
+                                                            const __grid_constant__ TmaMaps maps) {
+  extern __shared__ __align__(128) float4 tile_smem[];
+  float* smem = reinterpret_cast<float*>(tile_smem);
+  if (TMA) {
+    __shared__ __align__(8) unsigned long long mbar;
+    if (threadIdx.x == 0) mbar_init(smem_u32(&mbar), 1);
+    __syncthreads();
+    TmaCtx ctx{maps.map, smem_u32(&mbar),
+               reinterpret_cast<unsigned char*>(tile_smem) + ((Prog::smem_bytes + 127) & ~(size_t)127)};
+    Prog::run(p, blockIdx.x * kTileW, blockIdx.y * kTileH, smem, &ctx);
+  } else {
+    Prog::run(p, blockIdx.x * kTileW, blockIdx.y * kTileH, smem, nullptr);
+  }
 }
+
+bool encode_plane_map(CUtensorMap* map, const void* base, int W, int H, int pitch, int dtype, int box_w,
+                      int box_h);
 
 template <class Prog>
 int launch_tiles(const RavuArgs& a, int tiles_w, int tiles_h, cudaStream_t s) {
-  constexpr size_t smem = Prog::smem_bytes;
-  static_assert(smem <= 48 * 1024, "tile program needs more than the default shared memory");
-  tile_kernel<Prog><<<dim3(tiles_w, tiles_h), kTileThreads, smem, s>>>(a);
+  static_assert(Prog::smem_bytes <= 48 * 1024, "tile program needs more than the default shared memory");
+  TmaMaps maps;
+  std::memset(&maps, 0, sizeof maps);
+  if constexpr (Prog::kPlanes > 0) {
+    if (a.staging == 1) {
+      constexpr int BW = tma_box_w<Prog::TW>(), BH = Prog::TH;
+      const int dt = sizeof(typename Prog::Elem) == 4 ? 0 : 1;
+      bool ok = true;
+      for (int c = 0; c < Prog::kPlanes && ok; c++)
+        ok = encode_plane_map(&maps.map[c], a.in[c], a.W, a.H, a.in_pitch[c], dt, BW, BH);
+      if (ok) {
+        constexpr size_t smem = ((Prog::smem_bytes + 127) & ~(size_t)127) +
+                                (size_t)Prog::kPlanes * tma_plane_bytes<Prog::TW, Prog::TH, typename Prog::Elem>();
+        static_assert(smem <= 48 * 1024, "TMA staging needs more than the default shared memory");
+        tile_kernel<Prog, true><<<dim3(tiles_w, tiles_h), kTileThreads, smem, s>>>(a, maps);
+        return 0;
+      }
+    }
+  }
+  tile_kernel<Prog, false><<<dim3(tiles_w, tiles_h), kTileThreads, Prog::smem_bytes, s>>>(a, maps);
   return 0;
 }
 

@@ -37,6 +37,8 @@ _FAMILY_CODE = {"lite": _ffi.PZ_RAVU_LITE, "ravu": _ffi.PZ_RAVU, "zoom": _ffi.PZ
                 "3x": _ffi.PZ_RAVU_3X, "nnedi3": _ffi.PZ_NNEDI3}
 _CHANNEL_CODE = {"luma": _ffi.PZ_LUMA, "yuv": _ffi.PZ_YUV, "rgb": _ffi.PZ_RGB}
 PRECISIONS = {"fp32": _ffi.PZ_PREC_FP32, "fast": _ffi.PZ_PREC_FAST}
+# RAVU halo staging: clamped loads, or TMA boxes for interior tiles
+STAGINGS = {"ldg": 0, "tma": 1}
 
 
 def _torch():
@@ -198,7 +200,7 @@ class HookModel:
 
     # ---- execution ----------------------------------------------------
     def upscale(self, planes: PlaneLike, out_size: Optional[Tuple[int, int]] = None, precision: str = "fp32",
-                out=None, return_keys: bool = False, stream=None):
+                out=None, return_keys: bool = False, stream=None, staging: str = "ldg"):
         """Run the hook chain on ``planes``.
 
         ``planes``: a CUDA tensor ``[H][W]`` (luma), ``[C][H][W]`` (C = 1
@@ -208,6 +210,9 @@ class HookModel:
         otherwise it only decides the ``//!WHEN`` conditions.
         ``precision``: "fp32" (plain FP32 arithmetic) or "fast" (FP16
         tensor-core NNEDI3 neurons; RAVU arithmetic stays FP32).
+        ``staging``: how RAVU tiles stage their input window: "ldg"
+        (clamped loads) or "tma" (TMA boxes for interior tiles); the pixels
+        are identical, only the speed differs (see ``batch.autotune_staging``).
         Returns the upscaled planes in the input's form (and the raw LUT
         keys as int32 when ``return_keys``).
         """
@@ -215,7 +220,8 @@ class HookModel:
         if not isinstance(planes, (list, tuple)) and planes.dim() == 4:
             # a batch of frames [N][C][H][W]: one chain per frame, same stream
             outs = [self.upscale(f, out_size=out_size, precision=precision,
-                                 out=None if out is None else out[i], return_keys=return_keys, stream=stream)
+                                 out=None if out is None else out[i], return_keys=return_keys, stream=stream,
+                                 staging=staging)
                     for i, f in enumerate(planes.unbind(0))]
             if return_keys:
                 return torch.stack([o[0] for o in outs]), torch.stack([o[1] for o in outs])
@@ -245,7 +251,8 @@ class HookModel:
             keys = None
             if return_keys:
                 keys = torch.empty(self.key_shape(W, H, OW, OH), dtype=torch.int32, device=dev)
-            self.run_raw(pl, res, out_size=(OW, OH), precision=precision, keys=keys, stream=stream)
+            self.run_raw(pl, res, out_size=(OW, OH), precision=precision, keys=keys, stream=stream,
+                         staging=staging)
         return self._pack(res, planes, as_list, keys, return_keys)
 
     def upscale_host(self, frames, out=None, out_size: Optional[Tuple[int, int]] = None, precision: str = "fp32",
@@ -308,7 +315,7 @@ class HookModel:
             return (1,)
         return (H, W)
 
-    def run_raw(self, pl, res, out_size, precision="fp32", keys=None, stream=None, scratch=None):
+    def run_raw(self, pl, res, out_size, precision="fp32", keys=None, stream=None, scratch=None, staging="ldg"):
         """Low-level call of ``pz_run`` on prepared tensors (no allocation
         besides the optional NNEDI3 scratch inside the library)."""
         torch = _torch()
@@ -329,6 +336,7 @@ class HookModel:
         if scratch is not None:
             o.scratch = scratch.data_ptr()
             o.scratch_bytes = scratch.numel() * scratch.element_size()
+        o.staging = STAGINGS[staging]
         s = stream if stream is not None else torch.cuda.current_stream(pl[0].device)
         h = self.device_handle(pl[0].device.index)
         _ffi.check(_ffi.lib().pz_run(h, pin, n, pout, n, _ffi.ctypes.byref(o), s.cuda_stream))

@@ -218,9 +218,6 @@ def warmup_trace(models: Dict[str, HookModel], resolutions=RESOLUTIONS, algorith
     """One request of every (resolution, algorithm) pair, back to back, so that
     every kernel is loaded and the pinned host buffers of every output size
     are cached before a measured trace."""
-    reqs = poisson_trace(models, 1, resolutions=resolutions, algorithms=algorithms, precision=precision,
-                         frame_pool=1)
-    from . import synth
     torch = _torch()
     out, rid = [], 0
     for W, H, _ in resolutions:
@@ -230,7 +227,6 @@ def warmup_trace(models: Dict[str, HookModel], resolutions=RESOLUTIONS, algorith
             osz = (int(round(W * zoom)), int(round(H * zoom))) if zoom else None
             out.append(Request(rid, 0, name, f, 0.0, osz, precision))
             rid += 1
-    del reqs, synth
     return out
 
 

@@ -45,3 +45,32 @@ def test_when_false_leaves_planes_untouched():
     nn, _ = synth.model_for("nnedi3-nns16-win8x4")
     y = nn.upscale(x, out_size=(60, 80))  # rows only
     assert y.shape == (80, 60)
+
+
+@pytest.mark.parametrize("name", ["ravu-lite-ar-r4", "ravu-lite-r2", "ravu-r3", "ravu-r4-rgb", "ravu-3x-r3-yuv",
+                                  "ravu-zoom-ar-r2"])
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float16])
+def test_tma_staging_gives_identical_pixels(name, dtype):
+    """Interior tiles staged by TMA boxes, border tiles by clamped loads: the
+    same pixels as clamped loads everywhere (zoom always uses clamped loads)."""
+    hm, _ = synth.model_for(name)
+    x = torch.from_numpy(synth.frame(100, 216, 61, hm.channels)).to("cuda", dtype)
+    osz = (400, 180) if hm.family == "zoom" else None
+    a = hm.upscale(x, out_size=osz, staging="ldg")
+    b = hm.upscale(x, out_size=osz, staging="tma")
+    assert torch.equal(a, b)
+
+
+def test_tma_staging_falls_back_for_unaligned_pitch():
+    hm, _ = synth.model_for("ravu-lite-ar-r3")
+    big = torch.from_numpy(synth.luma_plane(90, 203, 62)).cuda()   # pitch 203 floats: not 16-byte rows
+    view = big[:, :200]
+    assert torch.equal(hm.upscale(view, staging="tma"), hm.upscale(view.contiguous(), staging="ldg"))
+
+
+def test_staging_autotuner(tmp_path):
+    from mpv_prescalers_gb300 import batch as B
+    hm, _ = synth.model_for("ravu-lite-ar-r3")
+    x = torch.rand((270, 480), device="cuda", dtype=torch.float16)
+    best, times = B.autotune_staging(hm, x, cache=B.PlanCache(str(tmp_path / "p.json")), reps=2)
+    assert best in ("ldg", "tma") and set(times) == {"ldg", "tma"}
