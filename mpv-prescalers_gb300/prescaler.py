@@ -200,7 +200,7 @@ class HookModel:
 
     # ---- execution ----------------------------------------------------
     def upscale(self, planes: PlaneLike, out_size: Optional[Tuple[int, int]] = None, precision: str = "fp32",
-                out=None, return_keys: bool = False, stream=None, staging: str = "ldg"):
+                out=None, return_keys: bool = False, stream=None, staging: str = "tma"):
         """Run the hook chain on ``planes``.
 
         ``planes``: a CUDA tensor ``[H][W]`` (luma), ``[C][H][W]`` (C = 1
@@ -315,7 +315,7 @@ class HookModel:
             return (1,)
         return (H, W)
 
-    def run_raw(self, pl, res, out_size, precision="fp32", keys=None, stream=None, scratch=None, staging="ldg"):
+    def run_raw(self, pl, res, out_size, precision="fp32", keys=None, stream=None, scratch=None, staging="tma"):
         """Low-level call of ``pz_run`` on prepared tensors (no allocation
         besides the optional NNEDI3 scratch inside the library)."""
         torch = _torch()
