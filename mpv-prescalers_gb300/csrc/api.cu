@@ -166,11 +166,14 @@ int pz_model_create(const pz_model_desc* d, pz_model** out) {
       bias[2 * k] = d->bias_a[k];
       bias[2 * k + 1] = d->bias_b[k];
     }
-    // tensor-core operand B [2*nns][T] FP16: rows 0..nns-1 softmax branch,
-    // nns..2nns-1 Elliott branch, stored as no-swizzle K-major core matrices
+    // tensor-core operand B [2*nns][T] FP16, chunk-major: chunk c of NC
+    // neurons (NC = 32, or 16 for nns16) is NC softmax-branch rows followed by
+    // NC Elliott-branch rows; stored as no-swizzle K-major core matrices
     // (8 rows x 8 halves; K-neighbours 64 halves apart, 8-row groups 8*T apart)
+    const int NC = n < 32 ? n : 32;
     for (int r = 0; r < 2 * n; r++) {
-      const int k = r % n, br = r / n;
+      const int chunk = r / (2 * NC), within = r % (2 * NC);
+      const int k = chunk * NC + within % NC, br = within / NC;
       for (int t = 0; t < T; t++)
         wh[(size_t)(r >> 3) * 8 * T + (t >> 3) * 64 + (r & 7) * 8 + (t & 7)] =
             __float2half_rn(w[((size_t)k * 2 + br) * T + t]);

@@ -89,44 +89,54 @@ __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence:
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
+// Neurons are processed in chunks of NC (32, or 16 for nns16): chunk k's
+// accumulator holds NC softmax-branch and NC Elliott-branch columns, and two
+// chunk buffers alternate in tensor memory (4*NC columns per CTA), so up to
+// four CTAs share an SM's 512 columns.  The MMA of chunk k+2 is issued as
+// soon as every warp has read chunk k, and runs under chunk k's epilogue.
+// Operand B is stored chunk-major: rows [2*NC*k, 2*NC*k + NC) are the
+// softmax weights of neurons k*NC.., the next NC rows their Elliott weights.
 template <int WH, int NNS, bool XP, typename T>
 __global__ void __launch_bounds__(kThreads) nn_tc_kernel(const __grid_constant__ NnArgs p) {
   constexpr int NT = 8 * WH;                 // K
-  constexpr int NCOL = 2 * NNS;              // accumulator columns
-  constexpr int NHALF = NCOL > 256 ? 256 : NCOL;
+  constexpr int NC = NNS < 32 ? NNS : 32;    // neurons per chunk
+  constexpr int NCH = NNS / NC;              // chunks per tile
+  constexpr int CCOL = 2 * NC;               // TMEM columns per chunk buffer
+  constexpr int TCOLS = 2 * CCOL;            // two buffers
   constexpr int DY0 = -(WH / 2 - 1);
   constexpr int OX0 = XP ? DY0 : -3, OX1 = XP ? WH / 2 : 4;
   constexpr int OY0 = XP ? -3 : DY0, OY1 = XP ? 4 : WH / 2;
   constexpr int TW = 32 + OX1 - OX0, TH = 4 + OY1 - OY0;
   constexpr uint32_t SBO = NT * 16;          // bytes between 8-row groups (A and B)
   constexpr uint32_t LBO = 128;              // bytes between K-adjacent core matrices
+  static_assert(NNS % NC == 0 && NC % 16 == 0, "neuron count must be a multiple of 16");
 
   extern __shared__ __align__(1024) unsigned char smem[];
-  unsigned char* sB = smem;                                  // [NCOL x NT] f16, 2*NNS*NT*2 bytes
-  unsigned char* sA = sB + NCOL * NT * 2;                    // [128 x NT] f16
+  unsigned char* sB = smem;                                    // [2*NNS x NT] f16
+  unsigned char* sA = sB + 2 * NNS * NT * 2;                   // [128 x NT] f16
   float4* aux = reinterpret_cast<float4*>(sA + 128 * NT * 2);  // [NNS] (csA, csB, bA, bB)
-  float* tile = reinterpret_cast<float*>(aux + NNS);         // [TH][TW]
-  __shared__ __align__(8) unsigned long long mbar;
+  float* tile = reinterpret_cast<float*>(aux + NNS);           // [TH][TW]
+  __shared__ __align__(8) unsigned long long mbar[2];
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  // ---- one-time setup: weights, TMEM, mbarrier
-  {
+  {  // one-time setup: weights, neuron constants
     const uint4* src = reinterpret_cast<const uint4*>(p.wts_h);
     uint4* dst = reinterpret_cast<uint4*>(sB);
-    for (int i = tid; i < NCOL * NT * 2 / 16; i += kThreads) dst[i] = __ldg(src + i);
+    for (int i = tid; i < 2 * NNS * NT * 2 / 16; i += kThreads) dst[i] = __ldg(src + i);
     for (int k = tid; k < NNS; k += kThreads)
       aux[k] = make_float4(__ldg(p.cs + 2 * k), __ldg(p.cs + 2 * k + 1), __ldg(p.bias + 2 * k),
                            __ldg(p.bias + 2 * k + 1));
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
-                 "r"(NCOL));
+                 "r"(TCOLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    mbar_init(smem_u32(&mbar), 1);
+    mbar_init(smem_u32(&mbar[0]), 1);
+    mbar_init(smem_u32(&mbar[1]), 1);
     abort_flag = 0;
   }
   fence_async_smem();
@@ -134,15 +144,25 @@ __global__ void __launch_bounds__(kThreads) nn_tc_kernel(const __grid_constant__
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_base;
-  const uint32_t mbar_a = smem_u32(&mbar);
+  const uint32_t mb0 = smem_u32(&mbar[0]), mb1 = smem_u32(&mbar[1]);
   const uint32_t a_addr = smem_u32(sA), b_addr = smem_u32(sB);
-  constexpr uint32_t IDESC = instr_desc(128, NHALF);
+  constexpr uint32_t IDESC = instr_desc(128, CCOL);
+  // D[buf] (+)= A x B[chunk]^T over the whole K; completion on mbar[buf]
+  auto issue_chunk = [&](int chunk, int buf) {
+#pragma unroll
+    for (int ks = 0; ks < NT / 16; ks++) {
+      const uint64_t ad = smem_desc(a_addr + ks * 2 * LBO, LBO, SBO);
+      const uint64_t bd = smem_desc(b_addr + (uint32_t)chunk * (CCOL / 8) * SBO + ks * 2 * LBO, LBO, SBO);
+      mma_f16(tmem + buf * CCOL, ad, bd, IDESC, ks > 0 ? 1u : 0u);
+    }
+    mma_commit(buf ? mb1 : mb0);
+  };
 
   const T* in = static_cast<const T*>(p.in);
   T* out = static_cast<T*>(p.out);
   const int tiles_x = (p.W + 31) / 32, tiles_y = (p.H + 3) / 4;
   const int ntiles = tiles_x * tiles_y;
-  uint32_t phase = 0;
+  uint32_t phase = 0;  // bit b: parity of mbar[b]'s next phase
 
   for (int tile_id = blockIdx.x; tile_id < ntiles; tile_id += gridDim.x) {
     const int x0 = (tile_id % tiles_x) * 32, y0 = (tile_id / tiles_x) * 4;
@@ -189,52 +209,50 @@ __global__ void __launch_bounds__(kThreads) nn_tc_kernel(const __grid_constant__
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    // ---- one thread issues the contraction
     if (tid == 0) {
-#pragma unroll
-      for (int ks = 0; ks < NT / 16; ks++) {
-        const uint64_t ad = smem_desc(a_addr + ks * 2 * LBO, LBO, SBO);
-#pragma unroll
-        for (int h = 0; h < NCOL / NHALF; h++) {
-          const uint64_t bd = smem_desc(b_addr + h * (NHALF / 8) * SBO + ks * 2 * LBO, LBO, SBO);
-          mma_f16(tmem + h * NHALF, ad, bd, IDESC, ks > 0 ? 1u : 0u);
-        }
-      }
-      mma_commit(mbar_a);
+      issue_chunk(0, 0);
+      if (NCH > 1) issue_chunk(1, 1);
     }
-    const bool ok = mbar_wait_bounded(mbar_a, phase);
-    phase ^= 1u;
-    if (!ok) atomicExch(&abort_flag, 1);
-    __syncthreads();
-    if (abort_flag) break;
-    tc_fence_after();
-    // ---- epilogue: lane m of TMEM holds pixel m's 2*NNS pre-activations
+    // ---- epilogue: lane m of TMEM holds pixel m's pre-activations
     const float mterm = mean * invstd;
     float wsum = 0.0f, vsum = 0.0f;
     const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
-    constexpr int CH = NNS < 32 ? NNS : 32;  // neurons per TMEM load (x16 or x32 columns)
 #pragma unroll 1
-    for (int c = 0; c < NNS; c += CH) {
+    for (int k = 0; k < NCH; k++) {
+      const int b = k & 1;
+      if (!mbar_wait_bounded(b ? mb1 : mb0, (phase >> b) & 1u)) atomicExch(&abort_flag, 1);
+      phase ^= 1u << b;
+      tc_fence_after();
       float s1[32], s2[32];
-      if (CH == 32) {
-        tmem_ld32(lane_addr + c, s1);
-        tmem_ld32(lane_addr + NNS + c, s2);
+      if (NC == 32) {
+        tmem_ld32(lane_addr + b * CCOL, s1);
+        tmem_ld32(lane_addr + b * CCOL + NC, s2);
       } else {
-        tmem_ld16(lane_addr + c, s1);
-        tmem_ld16(lane_addr + NNS + c, s2);
+        tmem_ld16(lane_addr + b * CCOL, s1);
+        tmem_ld16(lane_addr + b * CCOL + NC, s2);
       }
       tmem_wait_ld();
+      tc_fence_before();
+      __syncthreads();  // every warp has read buffer b
+      if (abort_flag) break;
+      if (tid == 0 && k + 2 < NCH) {
+        tc_fence_after();
+        issue_chunk(k + 2, b);
+      }
 #pragma unroll
-      for (int j = 0; j < CH; j++) {
-        const float4 q = aux[c + j];
-        const float a = s1[j] + mterm * q.x + q.z;
-        const float b = s2[j] + mterm * q.y + q.w;
-        const float e = __expf(a);
-        wsum += e;
-        vsum += e * __fdividef(b, 1.0f + fabsf(b));
+      for (int j = 0; j < NC; j += 2) {
+        const float4 q0 = aux[k * NC + j], q1 = aux[k * NC + j + 1];
+        const float a0 = s1[j] + mterm * q0.x + q0.z, a1 = s1[j + 1] + mterm * q1.x + q1.z;
+        const float b0 = s2[j] + mterm * q0.y + q0.w, b1 = s2[j + 1] + mterm * q1.y + q1.w;
+        const float e0 = __expf(a0), e1 = __expf(a1);
+        // b/(1+|b|) for two neurons from one reciprocal of the product
+        const float d0 = 1.0f + fabsf(b0), d1 = 1.0f + fabsf(b1);
+        const float r = __fdividef(1.0f, d0 * d1);
+        wsum += e0 + e1;
+        vsum += (e0 * b0 * d1 + e1 * b1 * d0) * r;
       }
     }
-    tc_fence_before();
+    if (abort_flag) break;
     const int gx = x0 + px, gy = y0 + py;
     if (gx < p.W && gy < p.H) {
       const float v = clampf(mean + 5.0f * vsum / wsum * stdv, 0.0f, 1.0f);
@@ -245,15 +263,14 @@ __global__ void __launch_bounds__(kThreads) nn_tc_kernel(const __grid_constant__
         stp(out + (size_t)(2 * gy + 1) * p.out_pitch + gx, v);
       }
     }
-    __syncthreads();  // TMEM and the A tile are free for the next tile
-    tc_fence_after();
+    __syncthreads();  // A tile and tile free for the next tile
   }
   if (abort_flag && tid == 0) atomicCAS(p.err, 0, kErrWaitTimeout);
   tc_fence_before();
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NCOL));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TCOLS));
   }
 }
 
@@ -262,10 +279,11 @@ int launch_one(const NnArgs& a, cudaStream_t s) {
   constexpr int NT = 8 * WH;
   constexpr int DY0 = -(WH / 2 - 1);
   constexpr int TW = 32 + (XP ? WH / 2 - DY0 : 7), TH = 4 + (XP ? 7 : WH / 2 - DY0);
-  // CTAs per SM are capped by tensor memory (512 columns per SM, 2*NNS per
+  // CTAs per SM are capped by tensor memory (512 columns per SM, 4*NC per
   // CTA): the shared-memory request is raised so that no more CTAs than fit
   // in TMEM can be resident, so tcgen05.alloc never waits on a neighbour.
-  constexpr int per_sm = (2 * NNS >= 512) ? 1 : (512 / (2 * NNS) > 4 ? 4 : 512 / (2 * NNS));
+  constexpr int NC = NNS < 32 ? NNS : 32;
+  constexpr int per_sm = 512 / (4 * NC) > 4 ? 4 : 512 / (4 * NC);
   int dev = 0, sms = 0, sm_smem = 0, blk_smem = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) return -95;
