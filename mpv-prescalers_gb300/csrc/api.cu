@@ -151,7 +151,8 @@ int pz_model_create(const pz_model_desc* d, pz_model** out) {
     m->win_h = d->win_h;
     const int T = d->win_w * d->win_h, n = d->nns;
     std::vector<float> w((size_t)n * 2 * T), cs((size_t)n * 2), bias((size_t)n * 2);
-    std::vector<__half> wh((size_t)n * 2 * T);
+    const int KP = (T + 3 + 15) / 16 * 16;  // taps + (mean term, bias hi, bias lo), padded to a K step
+    std::vector<__half> wh((size_t)n * 2 * KP, __float2half_rn(0.0f));
     for (int k = 0; k < n; k++) {
       double sa = 0, sb = 0;
       for (int t = 0; t < T; t++) {
@@ -166,17 +167,34 @@ int pz_model_create(const pz_model_desc* d, pz_model** out) {
       bias[2 * k] = d->bias_a[k];
       bias[2 * k + 1] = d->bias_b[k];
     }
-    // tensor-core operand B [2*nns][T] FP16, chunk-major: chunk c of NC
+    // tensor-core operand B [2*nns][KP] FP16, chunk-major: chunk c of NC
     // neurons (NC = 32, or 16 for nns16) is NC softmax-branch rows followed by
-    // NC Elliott-branch rows; stored as no-swizzle K-major core matrices
-    // (8 rows x 8 halves; K-neighbours 64 halves apart, 8-row groups 8*T apart)
+    // NC Elliott-branch rows.  Row = [weights (T taps), sum of the weights,
+    // bias hi, bias lo, 0...]; against A rows [x_hat, mean*invstd, 1, 1, 0...]
+    // the MMA yields the whole pre-activation <x,w>*invstd + b.  Softmax rows
+    // are scaled by log2(e) so the epilogue takes exp2 directly.  Stored as
+    // no-swizzle K-major core matrices (8 rows x 8 halves; K-neighbours 64
+    // halves apart, 8-row groups 8*KP apart).
     const int NC = n < 32 ? n : 32;
+    const double kLog2e = 1.4426950408889634;
     for (int r = 0; r < 2 * n; r++) {
       const int chunk = r / (2 * NC), within = r % (2 * NC);
       const int k = chunk * NC + within % NC, br = within / NC;
-      for (int t = 0; t < T; t++)
-        wh[(size_t)(r >> 3) * 8 * T + (t >> 3) * 64 + (r & 7) * 8 + (t & 7)] =
-            __float2half_rn(w[((size_t)k * 2 + br) * T + t]);
+      const double scale = br == 0 ? kLog2e : 1.0;
+      auto put = [&](int t, double v) {
+        wh[(size_t)(r >> 3) * 8 * KP + (t >> 3) * 64 + (r & 7) * 8 + (t & 7)] = __float2half_rn((float)v);
+      };
+      double sum = 0.0;
+      for (int t = 0; t < T; t++) {
+        const double v = w[((size_t)k * 2 + br) * T + t];
+        sum += v;
+        put(t, v * scale);
+      }
+      const double b = (br == 0 ? d->bias_a[k] : d->bias_b[k]) * scale;
+      const float bhi = __half2float(__float2half_rn((float)b));
+      put(T, sum * scale);
+      put(T + 1, bhi);
+      put(T + 2, b - bhi);
     }
     if ((rc = upload(&m->d_wts, w.data(), w.size() * 4)) || (rc = upload(&m->d_cs, cs.data(), cs.size() * 4)) ||
         (rc = upload(&m->d_bias, bias.data(), bias.size() * 4)) ||

@@ -84,6 +84,12 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[32]) {
   for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ float exp2f_approx(float x) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -98,7 +104,8 @@ __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.a
 // softmax weights of neurons k*NC.., the next NC rows their Elliott weights.
 template <int WH, int NNS, bool XP, typename T>
 __global__ void __launch_bounds__(kThreads) nn_tc_kernel(const __grid_constant__ NnArgs p) {
-  constexpr int NT = 8 * WH;                 // K
+  constexpr int NT = 8 * WH;                 // window taps
+  constexpr int KP = (NT + 3 + 15) / 16 * 16;  // K: taps, mean term, bias hi/lo, zero pad
   constexpr int NC = NNS < 32 ? NNS : 32;    // neurons per chunk
   constexpr int NCH = NNS / NC;              // chunks per tile
   constexpr int CCOL = 2 * NC;               // TMEM columns per chunk buffer
@@ -107,27 +114,23 @@ __global__ void __launch_bounds__(kThreads) nn_tc_kernel(const __grid_constant__
   constexpr int OX0 = XP ? DY0 : -3, OX1 = XP ? WH / 2 : 4;
   constexpr int OY0 = XP ? -3 : DY0, OY1 = XP ? 4 : WH / 2;
   constexpr int TW = 32 + OX1 - OX0, TH = 4 + OY1 - OY0;
-  constexpr uint32_t SBO = NT * 16;          // bytes between 8-row groups (A and B)
+  constexpr uint32_t SBO = KP * 16;          // bytes between 8-row groups (A and B)
   constexpr uint32_t LBO = 128;              // bytes between K-adjacent core matrices
   static_assert(NNS % NC == 0 && NC % 16 == 0, "neuron count must be a multiple of 16");
 
   extern __shared__ __align__(1024) unsigned char smem[];
-  unsigned char* sB = smem;                                    // [2*NNS x NT] f16
-  unsigned char* sA = sB + 2 * NNS * NT * 2;                   // [128 x NT] f16
-  float4* aux = reinterpret_cast<float4*>(sA + 128 * NT * 2);  // [NNS] (csA, csB, bA, bB)
-  float* tile = reinterpret_cast<float*>(aux + NNS);           // [TH][TW]
+  unsigned char* sB = smem;                                    // [2*NNS x KP] f16
+  unsigned char* sA = sB + 2 * NNS * KP * 2;                   // [128 x KP] f16
+  float* tile = reinterpret_cast<float*>(sA + 128 * KP * 2);   // [TH][TW]
   __shared__ __align__(8) unsigned long long mbar[2];
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  {  // one-time setup: weights, neuron constants
+  {  // one-time setup: the weight operand
     const uint4* src = reinterpret_cast<const uint4*>(p.wts_h);
     uint4* dst = reinterpret_cast<uint4*>(sB);
-    for (int i = tid; i < 2 * NNS * NT * 2 / 16; i += kThreads) dst[i] = __ldg(src + i);
-    for (int k = tid; k < NNS; k += kThreads)
-      aux[k] = make_float4(__ldg(p.cs + 2 * k), __ldg(p.cs + 2 * k + 1), __ldg(p.bias + 2 * k),
-                           __ldg(p.bias + 2 * k + 1));
+    for (int i = tid; i < 2 * NNS * KP * 2 / 16; i += kThreads) dst[i] = __ldg(src + i);
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
@@ -150,7 +153,7 @@ __global__ void __launch_bounds__(kThreads) nn_tc_kernel(const __grid_constant__
   // D[buf] (+)= A x B[chunk]^T over the whole K; completion on mbar[buf]
   auto issue_chunk = [&](int chunk, int buf) {
 #pragma unroll
-    for (int ks = 0; ks < NT / 16; ks++) {
+    for (int ks = 0; ks < KP / 16; ks++) {
       const uint64_t ad = smem_desc(a_addr + ks * 2 * LBO, LBO, SBO);
       const uint64_t bd = smem_desc(b_addr + (uint32_t)chunk * (CCOL / 8) * SBO + ks * 2 * LBO, LBO, SBO);
       mma_f16(tmem + buf * CCOL, ad, bd, IDESC, ks > 0 ? 1u : 0u);
@@ -194,14 +197,20 @@ __global__ void __launch_bounds__(kThreads) nn_tc_kernel(const __grid_constant__
     const float invstd = var >= kFltEps ? rsqrtf(var) : 0.0f;
     const float stdv = var * invstd;
     const float orig = tile[(py - OY0) * TW + px - OX0];
-    {
+    {  // A row: [x_hat (NT), mean * invstd, 1, 1, 0...]
       unsigned char* row = sA + (m >> 3) * SBO + (m & 7) * 16;
+      const float mterm = mean * invstd;
 #pragma unroll
-      for (int kc = 0; kc < NT / 8; kc++) {
+      for (int kc = 0; kc < KP / 8; kc++) {
         __half2 h[4];
 #pragma unroll
-        for (int j = 0; j < 4; j++)
-          h[j] = __floats2half2_rn(xv[8 * kc + 2 * j] * invstd, xv[8 * kc + 2 * j + 1] * invstd);
+        for (int j = 0; j < 4; j++) {
+          const int t = 8 * kc + 2 * j;
+          const float v0 = t < NT ? xv[t] * invstd : (t == NT ? mterm : (t <= NT + 2 ? 1.0f : 0.0f));
+          const float v1 = t + 1 < NT ? xv[t + 1] * invstd
+                                      : (t + 1 == NT ? mterm : (t + 1 <= NT + 2 ? 1.0f : 0.0f));
+          h[j] = __floats2half2_rn(v0, v1);
+        }
         *reinterpret_cast<uint4*>(row + kc * LBO) = *reinterpret_cast<uint4*>(h);
       }
     }
@@ -214,7 +223,7 @@ __global__ void __launch_bounds__(kThreads) nn_tc_kernel(const __grid_constant__
       if (NCH > 1) issue_chunk(1, 1);
     }
     // ---- epilogue: lane m of TMEM holds pixel m's pre-activations
-    const float mterm = mean * invstd;
+    // (softmax branch already in log2 units, Elliott branch as is)
     float wsum = 0.0f, vsum = 0.0f;
     const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
 #pragma unroll 1
@@ -241,10 +250,8 @@ __global__ void __launch_bounds__(kThreads) nn_tc_kernel(const __grid_constant__
       }
 #pragma unroll
       for (int j = 0; j < NC; j += 2) {
-        const float4 q0 = aux[k * NC + j], q1 = aux[k * NC + j + 1];
-        const float a0 = s1[j] + mterm * q0.x + q0.z, a1 = s1[j + 1] + mterm * q1.x + q1.z;
-        const float b0 = s2[j] + mterm * q0.y + q0.w, b1 = s2[j + 1] + mterm * q1.y + q1.w;
-        const float e0 = __expf(a0), e1 = __expf(a1);
+        const float b0 = s2[j], b1 = s2[j + 1];
+        const float e0 = exp2f_approx(s1[j]), e1 = exp2f_approx(s1[j + 1]);
         // b/(1+|b|) for two neurons from one reciprocal of the product
         const float d0 = 1.0f + fabsf(b0), d1 = 1.0f + fabsf(b1);
         const float r = __fdividef(1.0f, d0 * d1);
@@ -289,7 +296,8 @@ int launch_one(const NnArgs& a, cudaStream_t s) {
   if (dev < 0 || dev >= 64) return -95;
   cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
   cudaDeviceGetAttribute(&blk_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const size_t need = (size_t)2 * NNS * NT * 2 + 128 * NT * 2 + NNS * 16 + TW * TH * 4;
+  constexpr int KP = (NT + 3 + 15) / 16 * 16;
+  const size_t need = (size_t)2 * NNS * KP * 2 + 128 * KP * 2 + TW * TH * 4;
   const size_t cap = (size_t)sm_smem / (per_sm + 1) + 1024;
   const size_t smem = need > cap ? need : cap;
   if (smem > (size_t)blk_smem) return -95;
