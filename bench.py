@@ -366,8 +366,44 @@ def run_reference(args):
                     "the CPU restatement of their arithmetic (FP64 NumPy), all host cores"}
 
 
+# Single-kernel cases for profilers: (model, channels of the frame, out_size,
+# precision); one 1920x1080 FP16 frame, 3 warm-up + 3 measured calls.
+CASES = {
+    "ravu-lite-ar-r4": ("ravu-lite-ar-r4", None, "fp32"),
+    "ravu-lite-ar-r3": ("ravu-lite-ar-r3", None, "fp32"),
+    "ravu-r3": ("ravu-r3", None, "fp32"),
+    "ravu-r4-yuv": ("ravu-r4-yuv", None, "fp32"),
+    "ravu-zoom-ar-r2-rgb": ("ravu-zoom-ar-r2-rgb", (2880, 1620), "fp32"),
+    "ravu-3x-r3": ("ravu-3x-r3", None, "fp32"),
+    "nnedi3-nns128-win8x6-fast": ("nnedi3-nns128-win8x6", None, "fast"),
+    "nnedi3-nns128-win8x6-fp32": ("nnedi3-nns128-win8x6", None, "fp32"),
+}
+
+
+def run_case(name: str) -> None:
+    """Run one kernel case (for ncu captures; prints per-call ms)."""
+    import torch
+    _pkg()
+    from mpv_prescalers_gb300 import synth
+    model, out_size, prec = CASES[name]
+    hm, src = synth.model_for(model)
+    x = torch.from_numpy(synth.frame(H, W, SEED0, hm.channels)).to("cuda", torch.float16)
+    for _ in range(3):
+        hm.upscale(x, out_size=out_size, precision=prec)
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(3):
+        hm.upscale(x, out_size=out_size, precision=prec)
+    b.record()
+    torch.cuda.synchronize()
+    print(json.dumps({"case": name, "weights": src, "ms_per_call": a.elapsed_time(b) / 3}))
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--case", choices=sorted(CASES), help="run one single-kernel case and exit (profiling)")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
@@ -377,6 +413,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=480, help="requests in the serving trace (0: skip)")
     args = ap.parse_args()
+    if args.case:
+        run_case(args.case)
+        return
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
     if args.impl == "reference":
