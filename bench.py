@@ -68,7 +68,7 @@ def _cpu_strip(args):
     import oracle
     hm, _ = synth.model_for(name)
     x = synth.luma_plane(H, W, seed)
-    pad = 8
+    pad = 6  # covers the windows: lite r4 +-3, ravu r3 int11 (+-3) feeding the lattice (+-3)
     a, b = max(0, y0 - pad), min(H, y1 + pad)
     t = time.perf_counter()
     y, _ = oracle.keyed_upscale(hm.model, x[a:b])
@@ -151,6 +151,22 @@ class Clocks:
 
 # ------------------------------------------------------------------- GPU ---
 
+def max_over_ranks(ms: float, device=None) -> float:
+    """The slowest rank's time (replicas: the job ends with its last rank)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(out_px_per_rank_step: float, steps: int, ms: float, world: int) -> float:
+    """Whole-job Mpix/s: the pixels all ranks produced over the slowest rank's time."""
+    return world * out_px_per_rank_step * steps / (ms / 1e3) / 1e6
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -204,20 +220,15 @@ def run_gpu(args):
         t1.record(stream)
         torch.cuda.synchronize()
         barrier()
-        ms = t0.elapsed_time(t1)
-        if world > 1:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms
+        return max_over_ranks(t0.elapsed_time(t1), dev)
 
     out_px_step = len(MODELS) * NFRAMES * (2 * W) * (2 * H)
     kev = []
     clk = Clocks(local).__enter__()   # sampled over all three timed loops (device, FP32, end to end)
     ms16 = timed(x16, outs16, args.steps, args.warmup, kev)
     ms32 = timed(x32, outs32, args.steps, args.warmup)
-    value = world * out_px_step * args.steps / (ms16 / 1e3) / 1e6
-    fp32_value = world * out_px_step * args.steps / (ms32 / 1e3) / 1e6
+    value = job_value(out_px_step, args.steps, ms16, world)
+    fp32_value = job_value(out_px_step, args.steps, ms32, world)
     kern_ms = statistics.mean(a.elapsed_time(b) for a, b in kev)
 
     # ---- end to end: pinned host frames in, upscaled frames back, per step
@@ -244,9 +255,9 @@ def run_gpu(args):
     e1.record(stream)
     torch.cuda.synchronize()
     barrier()
-    e2e_ms = e0.elapsed_time(e1)
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1), dev)
     clk.__exit__(None, None, None)
-    e2e_value = world * out_px_step * args.steps / (e2e_ms / 1e3) / 1e6
+    e2e_value = job_value(out_px_step, args.steps, e2e_ms, world)
 
     # ---- headline pairs at 1080p -> 2160p (single frame, chosen vs FP32)
     headline = {}
@@ -345,7 +356,11 @@ def run_reference(args):
     if rank != 0:
         return None
     workers = len(os.sched_getaffinity(0))
-    rows = args.ref_rows
+    # each step is a bounded sample: rows per step are sized from a calibration
+    # run so that all steps together take about `ref_budget` seconds
+    calib = cpu_baseline(2 * workers, workers)
+    rows_per_s = 2 * workers * len(MODELS) / max(calib["seconds"], 1e-3) / len(MODELS)
+    rows = int(max(16, min(args.ref_rows, args.ref_budget / max(args.steps, 1) * rows_per_s)))
     for _ in range(max(0, min(args.warmup, 1))):
         cpu_baseline(16, workers)
     vals = []
@@ -409,7 +424,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-rows", type=int, default=1080, help="input rows per model in the CPU sample")
-    ap.add_argument("--ref-rows", type=int, default=540)
+    ap.add_argument("--ref-rows", type=int, default=540, help="largest CPU sample per reference step (input rows)")
+    ap.add_argument("--ref-budget", type=float, default=90.0, help="seconds of CPU work for all reference steps")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=480, help="requests in the serving trace (0: skip)")
     args = ap.parse_args()

@@ -36,6 +36,12 @@ def _torch():
     return torch
 
 
+def _pinned(t):
+    """Page-locked copy where a CUDA device exists (traces are also built on
+    hosts without one, e.g. to check their mix)."""
+    return t.pin_memory() if _torch().cuda.is_available() else t
+
+
 @dataclass
 class Request:
     rid: int
@@ -64,6 +70,26 @@ def request_bytes(model: HookModel, frame, out_size) -> int:
     if model.family == "nnedi3" and model.nnedi3_axes(W, H, (OW, OH)) == 3:
         nbytes += 2 * H * W * es
     return nbytes
+
+
+def admit_group(queue: List[Request], models: Dict[str, HookModel], budget: int, in_use: int,
+                max_group: int, rejected: List[Request]) -> Tuple[List[Request], int]:
+    """Take requests off the head of ``queue`` in arrival order while their
+    device bytes fit ``budget - in_use`` (at most ``max_group``).  A request
+    larger than the whole budget can never run: it moves to ``rejected``
+    instead of stalling the queue.  Returns the group and its bytes."""
+    group, nbytes = [], 0
+    while queue and len(group) < max_group:
+        r = queue[0]
+        need = request_bytes(models[r.model], r.frame, r.out_size)
+        if need > budget:
+            rejected.append(queue.pop(0))
+            continue
+        if in_use + nbytes + need > budget:
+            break
+        group.append(queue.pop(0))
+        nbytes += need
+    return group, nbytes
 
 
 @dataclass
@@ -149,19 +175,8 @@ class Server:
             for s in self.slots:
                 if s.reqs or not queue:
                     continue
-                group, nbytes = [], 0
-                while queue and len(group) < max_group:
-                    r = queue[0]
-                    need = request_bytes(self.models[r.model], r.frame, r.out_size)
-                    if need > self.budget:  # can never fit: refuse it rather than stall the queue
-                        self.rejected.append(queue.pop(0))
-                        continue
-                    if self.in_use + nbytes + need > self.budget:
-                        break
-                    group.append(queue.pop(0))
-                    nbytes += need
-                    if self.mode == "streams":
-                        break
+                group, nbytes = admit_group(queue, self.models, self.budget, self.in_use,
+                                            max_group if self.mode == "batch" else 1, self.rejected)
                 if not group:
                     break
                 self.in_use += nbytes
@@ -223,7 +238,7 @@ def warmup_trace(models: Dict[str, HookModel], resolutions=RESOLUTIONS, algorith
     for W, H, _ in resolutions:
         for name, zoom in algorithms:
             m = models[name]
-            f = torch.zeros((m.n_planes, H, W), dtype=torch.float16).pin_memory()
+            f = _pinned(torch.zeros((m.n_planes, H, W), dtype=torch.float16))
             osz = (int(round(W * zoom)), int(round(H * zoom))) if zoom else None
             out.append(Request(rid, 0, name, f, 0.0, osz, precision))
             rid += 1
@@ -248,8 +263,8 @@ def poisson_trace(models: Dict[str, HookModel], n: int, rate: float = 240.0, str
         key = (ri, channels)
         if key not in pool:
             W, H, _ = resolutions[ri]
-            pool[key] = [torch.from_numpy(synth.frame(H, W, seed + 17 * ri + j, channels)).to(torch.float16)
-                         .pin_memory() for j in range(frame_pool)]
+            pool[key] = [_pinned(torch.from_numpy(synth.frame(H, W, seed + 17 * ri + j, channels))
+                                 .to(torch.float16)) for j in range(frame_pool)]
         return pool[key][k % frame_pool]
 
     t = 0.0

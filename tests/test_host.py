@@ -1,0 +1,207 @@
+"""Host-side logic that needs no GPU: the plan cache, request sizing and
+admission, serving traces, batch job tables, and the bench's replica timing
+(max over ranks, checked with two ``gloo`` ranks on CPU)."""
+import json
+import os
+import socket
+
+import numpy as np
+import pytest
+
+from mpv_prescalers_gb300 import batch as B
+from mpv_prescalers_gb300 import serve as S
+from mpv_prescalers_gb300 import synth
+
+torch = pytest.importorskip("torch")
+
+
+# ------------------------------------------------------------ plan cache ---
+
+def _jobs(names_shapes, dtype=torch.float16, precision="fast"):
+    out = []
+    for name, (h, w), osz in names_shapes:
+        hm, _ = synth.model_for(name)
+        out.append(B.Job.make(hm, torch.zeros((hm.n_planes, h, w), dtype=dtype), out_size=osz, precision=precision))
+    return out
+
+
+def test_plan_cache_roundtrip(tmp_path):
+    path = str(tmp_path / "sub" / "plans.json")
+    c = B.PlanCache(path)
+    assert c.get("x") is None
+    c.put("gpu:abc", {"strategy": "batch:2", "times_ms": {"per_job": 1.5}})
+    assert json.load(open(path)) == {"gpu:abc": {"strategy": "batch:2", "times_ms": {"per_job": 1.5}}}
+    assert B.PlanCache(path).get("gpu:abc")["strategy"] == "batch:2"
+
+
+def test_plan_cache_tolerates_bad_files(tmp_path):
+    bad = tmp_path / "plans.json"
+    bad.write_text("{not json")
+    c = B.PlanCache(str(bad))
+    assert c.entries == {}
+    ro = tmp_path / "ro"
+    ro.mkdir()
+    os.chmod(ro, 0o500)
+    try:
+        c2 = B.PlanCache(str(ro / "deeper" / "plans.json"))
+        c2.put("k", {"strategy": "per_job"})       # no exception: only persistence is lost
+        assert c2.get("k") == {"strategy": "per_job"}
+    finally:
+        os.chmod(ro, 0o700)
+
+
+def test_plan_cache_key_is_order_free_and_shape_sensitive():
+    a = _jobs([("ravu-lite-ar-r3", (40, 60), None), ("nnedi3-nns16-win8x4", (20, 30), None)])
+    b = list(reversed(a))
+    assert B.PlanCache.key("GB300", a) == B.PlanCache.key("GB300", b)
+    c = _jobs([("ravu-lite-ar-r3", (40, 62), None), ("nnedi3-nns16-win8x4", (20, 30), None)])
+    assert B.PlanCache.key("GB300", a) != B.PlanCache.key("GB300", c)
+    d = _jobs([("ravu-lite-ar-r3", (40, 60), None), ("nnedi3-nns16-win8x4", (20, 30), None)], precision="fp32")
+    assert B.PlanCache.key("GB300", a) != B.PlanCache.key("GB300", d)
+    assert B.PlanCache.key("GB300", a) != B.PlanCache.key("B200", a)
+
+
+# ------------------------------------------------------------ batch jobs ---
+
+@pytest.mark.parametrize("name,shape,osz,want,scratch", [
+    ("ravu-lite-ar-r3", (36, 52), None, (72, 104), None),
+    ("ravu-r4-rgb", (20, 30), None, (40, 60), None),
+    ("ravu-3x-r3-yuv", (20, 30), None, (60, 90), None),
+    ("ravu-zoom-ar-r2", (30, 40), (70, 51), (51, 70), None),
+    ("nnedi3-nns16-win8x4", (20, 30), None, (40, 60), 2 * 20 * 30 * 2),
+    ("nnedi3-nns16-win8x4", (20, 30), (30, 40), (40, 30), None),      # rows only: no intermediate plane
+])
+def test_job_make_shapes(name, shape, osz, want, scratch):
+    hm, _ = synth.model_for(name)
+    x = torch.zeros((hm.n_planes,) + shape, dtype=torch.float16)
+    j = B.Job.make(hm, x, out_size=osz)
+    assert len(j.inputs) == len(j.outputs) == hm.n_planes
+    assert all(tuple(o.shape) == want for o in j.outputs)
+    # one allocation for all planes of a frame, planes back to back
+    if hm.n_planes > 1:
+        assert j.outputs[1].data_ptr() - j.outputs[0].data_ptr() == want[0] * want[1] * 2
+    assert (j.scratch is None) == (scratch is None)
+    if scratch is not None:
+        assert j.scratch.numel() == scratch
+    assert j.out_size == (want[1], want[0])
+
+
+# ----------------------------------------------- request sizing / admission --
+
+def test_request_bytes():
+    lite, _ = synth.model_for("ravu-lite-ar-r3")
+    f = torch.zeros((1, 100, 200), dtype=torch.float16)
+    assert S.request_bytes(lite, f, None) == (100 * 200 + 200 * 400) * 2
+    rgb, _ = synth.model_for("ravu-r4-rgb")
+    f3 = torch.zeros((3, 100, 200), dtype=torch.float32)
+    assert S.request_bytes(rgb, f3, None) == 3 * (100 * 200 + 200 * 400) * 4
+    nn, _ = synth.model_for("nnedi3-nns64-win8x4")
+    assert S.request_bytes(nn, f, None) == (100 * 200 + 200 * 400 + 2 * 100 * 200) * 2
+    zoom, _ = synth.model_for("ravu-zoom-ar-r2")
+    assert S.request_bytes(zoom, f, (350, 175)) == (100 * 200 + 350 * 175) * 2
+
+
+def _req(rid, model, h, w, arrival=0.0, osz=None):
+    hm, _ = synth.model_for(model)
+    return S.Request(rid, 0, model, torch.zeros((hm.n_planes, h, w), dtype=torch.float16), arrival, osz)
+
+
+def test_admission_respects_budget_and_order():
+    models = {n: synth.model_for(n)[0] for n in ("ravu-lite-ar-r3", "nnedi3-nns64-win8x4")}
+    one = (100 * 200 + 200 * 400) * 2                         # a lite request's bytes
+    q = [_req(i, "ravu-lite-ar-r3", 100, 200) for i in range(5)]
+    rejected = []
+    g, nb = S.admit_group(q, models, budget=3 * one, in_use=0, max_group=4, rejected=rejected)
+    assert [r.rid for r in g] == [0, 1, 2] and nb == 3 * one and [r.rid for r in q] == [3, 4]
+    g, nb = S.admit_group(q, models, budget=3 * one, in_use=3 * one, max_group=4, rejected=rejected)
+    assert g == [] and nb == 0 and len(q) == 2                # full: nothing admitted, nothing lost
+    g, nb = S.admit_group(q, models, budget=3 * one, in_use=2 * one, max_group=1, rejected=rejected)
+    assert [r.rid for r in g] == [3] and rejected == []
+
+
+def test_admission_rejects_requests_larger_than_budget():
+    models = {n: synth.model_for(n)[0] for n in ("ravu-lite-ar-r3",)}
+    small = (10 * 20 + 20 * 40) * 2
+    q = [_req(0, "ravu-lite-ar-r3", 1000, 2000), _req(1, "ravu-lite-ar-r3", 10, 20)]
+    rejected = []
+    g, nb = S.admit_group(q, models, budget=small, in_use=0, max_group=4, rejected=rejected)
+    assert [r.rid for r in rejected] == [0]
+    assert [r.rid for r in g] == [1] and nb == small and q == []
+
+
+# ---------------------------------------------------------------- traces ---
+
+def _trace_models():
+    return {n: synth.model_for(n)[0] for n, _ in S.ALGORITHMS}
+
+
+def test_poisson_trace_is_seeded_and_has_the_mix():
+    models = _trace_models()
+    res = ((64, 36, 0.5), (96, 54, 0.5))
+    a = S.poisson_trace(models, 400, rate=200.0, streams=16, seed=11, resolutions=res)
+    b = S.poisson_trace(models, 400, rate=200.0, streams=16, seed=11, resolutions=res)
+    assert [(r.arrival, r.model, r.stream_id, r.out_size, tuple(r.frame.shape)) for r in a] == \
+           [(r.arrival, r.model, r.stream_id, r.out_size, tuple(r.frame.shape)) for r in b]
+    assert all(torch.equal(x.frame, y.frame) for x, y in zip(a, b))
+    arr = np.array([r.arrival for r in a])
+    assert np.all(np.diff(arr) > 0)
+    assert 150 < len(a) / arr[-1] < 260                       # ~200 requests/s
+    # a stream keeps its model and resolution
+    per_stream = {}
+    for r in a:
+        per_stream.setdefault(r.stream_id, set()).add((r.model, tuple(r.frame.shape[-2:])))
+    assert all(len(v) == 1 for v in per_stream.values())
+    for r in a:
+        assert r.frame.shape[0] == models[r.model].n_planes and r.frame.dtype == torch.float16
+        if r.model == "ravu-zoom-ar-r2":
+            h, w = r.frame.shape[-2:]
+            assert r.out_size == (int(round(w * 1.75)), int(round(h * 1.75)))
+        else:
+            assert r.out_size is None
+    c = S.poisson_trace(models, 400, rate=200.0, streams=16, seed=12, resolutions=res)
+    assert [r.arrival for r in c] != [r.arrival for r in a]
+
+
+def test_warmup_trace_covers_every_pair():
+    models = _trace_models()
+    res = ((64, 36, 0.5), (96, 54, 0.5))
+    t = S.warmup_trace(models, resolutions=res)
+    assert {(r.model, tuple(r.frame.shape[-2:])) for r in t} == \
+           {(n, (h, w)) for w, h, _ in res for n, _ in S.ALGORITHMS}
+
+
+def test_summarize():
+    done = []
+    for i, lat in enumerate([0.001, 0.002, 0.003, 0.010]):
+        r = S.Request(i, 0, "m", None, arrival=0.01 * i)
+        r.finish = r.arrival + lat
+        r.output = torch.zeros((1, 20, 30))
+        done.append(r)
+    s = S.summarize(done, peak_bytes=5e9)
+    assert s["requests"] == 4 and s["max_ms"] == pytest.approx(10.0)
+    assert s["p50_ms"] == pytest.approx(2.5) and s["peak_hbm_gb"] == 5.0
+    assert s["out_mpix_s"] == pytest.approx(4 * 600 / 0.04 / 1e6)
+
+
+# ------------------------------------------------ bench replica timing (gloo) --
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def test_bench_replica_timing_is_max_over_ranks(tmp_path):
+    import torch.multiprocessing as tmp
+    from replica_worker import rank_main
+    tmp.spawn(rank_main, args=(2, _free_port(), str(tmp_path)), nprocs=2, join=True)
+    got = [json.load(open(tmp_path / f"r{r}.json")) for r in range(2)]
+    for g in got:
+        assert g["ms"] == 17.5
+        assert g["value"] == pytest.approx(2 * 1000.0 * 4 / 0.0175 / 1e6)
+
+
+def test_bench_replica_timing_single_process():
+    import bench
+    assert bench.max_over_ranks(3.25) == 3.25
+    assert bench.job_value(2e6, 10, 1000.0, 1) == pytest.approx(20.0)
