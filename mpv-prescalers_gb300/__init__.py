@@ -9,10 +9,12 @@ The arithmetic runs in hand-written sm_103a CUDA kernels inside
 hook files and drives the library through ctypes.
 """
 from .hookfile import HookParseError, parse_hook_file, parse_hook_text, rpn_eval  # noqa: F401
+from .hookwriter import format_hook, model_to_hook, write_hook  # noqa: F401
 from .models import Nnedi3Model, RavuModel, load_model  # noqa: F401
 from .prescaler import (PRECISIONS, HookModel, build_model_cache, cached_model, load_hook,  # noqa: F401
                         MODEL_DIR)
 from ._ffi import PrescaleError, PrescaleLibraryError  # noqa: F401
 
 __all__ = ["load_hook", "HookModel", "cached_model", "build_model_cache", "parse_hook_file",
+           "format_hook", "model_to_hook", "write_hook",
            "HookParseError", "PrescaleError", "PrescaleLibraryError"]

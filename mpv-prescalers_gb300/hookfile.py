@@ -68,6 +68,7 @@ class HookFile:
     path: str
     passes: List[Pass]
     textures: Dict[str, Texture]
+    preamble: List[str] = dataclasses.field(default_factory=list)   # lines before the first block
 
     @property
     def style(self) -> str:
@@ -107,6 +108,8 @@ def parse_hook_text(text: str, path: str = "<string>") -> HookFile:
     textures: Dict[str, Texture] = {}
     cur: Optional[dict] = None
     tex: Optional[dict] = None
+    preamble: List[str] = []
+    seen_block = False
 
     def close_pass():
         nonlocal cur
@@ -127,6 +130,7 @@ def parse_hook_text(text: str, path: str = "<string>") -> HookFile:
             if not m:
                 raise HookParseError(path, lineno, "malformed directive")
             key, val = m.group(1), m.group(2).strip()
+            seen_block = seen_block or key in ("DESC", "TEXTURE")
             if key == "DESC":
                 close_pass()
                 tex = None
@@ -192,6 +196,8 @@ def parse_hook_text(text: str, path: str = "<string>") -> HookFile:
             cur["body"].append(ln)
         elif tex is not None and ln.strip():
             raise HookParseError(path, lineno, "unexpected text inside texture block")
+        elif not seen_block:
+            preamble.append(ln)
         i += 1
     close_pass()
     if not passes:
@@ -203,7 +209,7 @@ def parse_hook_text(text: str, path: str = "<string>") -> HookFile:
             if any(q.save == b for q in passes):
                 continue
             raise HookParseError(path, p.line, f"pass binds unknown texture {b!r}")
-    return HookFile(path=path, passes=passes, textures=textures)
+    return HookFile(path=path, passes=passes, textures=textures, preamble=preamble)
 
 
 def parse_hook_file(path: str) -> HookFile:
