@@ -64,7 +64,13 @@ typedef enum { PZ_F32 = 0, PZ_F16 = 1 } pz_dtype;
 
 typedef enum {
   PZ_PREC_FP32 = 0,  /* plain FP32 arithmetic everywhere                    */
-  PZ_PREC_FAST = 1   /* FP16 tensor-core NNEDI3 neurons; RAVU unchanged     */
+  PZ_PREC_FAST = 1,  /* FP16 tensor-core NNEDI3 neurons; RAVU unchanged     */
+  PZ_PREC_MPV = 2    /* what the mpv host computes, to measure the distance
+                        to it: RAVU LUTs rounded to FP16 as the host uploads
+                        them (//!FORMAT rgba16f, ravu-lite-r3.hook:134),
+                        ravu-zoom LUT bilinear weights in 1/256 steps as the
+                        texture unit forms them; FP16 planes only (the
+                        host's textures are rgba16f); NNEDI3 as PZ_PREC_FP32 */
 } pz_precision;
 
 /* Everything a .hook file contributes; host arrays are copied. */
@@ -188,6 +194,24 @@ int pz_batch_run(const pz_job* jobs, int n_jobs, void* work, size_t work_bytes,
 #define PZ_STATIC_SCRATCH_BYTES (16u * 1024u * 1024u)
 int pz_nnedi3_run_static(const pz_model* model, const pz_plane* in, pz_plane* out,
                          const pz_opts* opts, void* cuda_stream);
+
+/* ---- resampling around the hook chain ---------------------------------
+ * The scaler steps a host performs around a prescaler, for callers that want
+ * the picture the host would show:
+ *   - the shift a pass announces with //!OFFSET (ravu-r3.hook:424
+ *     "-0.5 -0.5"; nnedi3-nns16-win8x4.hook:95 "0 -0.5", :185
+ *     "-0.5 0"), which mpv folds into its next scaling pass: sx = sy = 1,
+ *     (ox, oy) = the accumulated offset;
+ *   - chroma upsampling (--cscale) that merges subsampled planes before a
+ *     NATIVE hook (compute/ravu-r2-yuv.hook:15; README.md:50-56): sx, sy =
+ *     chroma/luma size ratio, ox, oy = -(chroma siting in luma px) * ratio.
+ * out(x, y) = sum k(u - i) k(v - j) in(clamp(i), clamp(j)) with
+ * u = sx * x + ox, v = sy * y + oy, texel centres at integers, edges
+ * replicated; k = bilinear tent or Catmull-Rom cubic.  Any sizes; in and
+ * out share one dtype; asynchronous on the stream. */
+typedef enum { PZ_FILTER_BILINEAR = 0, PZ_FILTER_CATMULL_ROM = 1 } pz_filter;
+int pz_resample(const pz_plane* in, pz_plane* out, float sx, float ox, float sy, float oy, int filter,
+                void* cuda_stream);
 
 #ifdef __cplusplus
 }

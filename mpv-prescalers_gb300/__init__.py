@@ -10,6 +10,7 @@ hook files and drives the library through ctypes.
 """
 from .hookfile import HookParseError, parse_hook_file, parse_hook_text, rpn_eval  # noqa: F401
 from .hookwriter import format_hook, model_to_hook, write_hook  # noqa: F401
+from .frame import Frame, plan_frame, prescale_frame, resample_plane  # noqa: F401
 from .models import Nnedi3Model, RavuModel, load_model  # noqa: F401
 from .prescaler import (PRECISIONS, HookModel, build_model_cache, cached_model, load_hook,  # noqa: F401
                         MODEL_DIR)
@@ -17,4 +18,5 @@ from ._ffi import PrescaleError, PrescaleLibraryError  # noqa: F401
 
 __all__ = ["load_hook", "HookModel", "cached_model", "build_model_cache", "parse_hook_file",
            "format_hook", "model_to_hook", "write_hook",
+           "Frame", "plan_frame", "prescale_frame", "resample_plane",
            "HookParseError", "PrescaleError", "PrescaleLibraryError"]

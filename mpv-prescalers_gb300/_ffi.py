@@ -23,7 +23,8 @@ PZ_ETIMEDOUT = -110
 PZ_RAVU_LITE, PZ_RAVU, PZ_RAVU_ZOOM, PZ_RAVU_3X, PZ_NNEDI3 = 1, 2, 3, 4, 5
 PZ_LUMA, PZ_YUV, PZ_RGB = 0, 1, 2
 PZ_F32, PZ_F16 = 0, 1
-PZ_PREC_FP32, PZ_PREC_FAST = 0, 1
+PZ_PREC_FP32, PZ_PREC_FAST, PZ_PREC_MPV = 0, 1, 2
+PZ_FILTER_BILINEAR, PZ_FILTER_CATMULL_ROM = 0, 1
 
 
 class PrescaleLibraryError(RuntimeError):
@@ -85,6 +86,8 @@ EXPORTS = {
                                     ctypes.c_void_p]),
     "pz_nnedi3_run_static": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Plane), ctypes.POINTER(Plane),
                                             ctypes.POINTER(Opts), ctypes.c_void_p]),
+    "pz_resample": (ctypes.c_int, [ctypes.POINTER(Plane), ctypes.POINTER(Plane), ctypes.c_float, ctypes.c_float,
+                                   ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_void_p]),
 }
 
 # Size of the static intermediate-plane array behind pz_nnedi3_run_static.

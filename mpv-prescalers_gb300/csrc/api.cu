@@ -270,14 +270,23 @@ int pz_model_create(const pz_model_desc* d, pz_model** out) {
   }
   m->lut_rows = d->lut_rows;
   m->lut_cols = d->lut_cols;
-  const size_t bytes = (size_t)d->lut_rows * d->lut_cols * 16;
-  if ((rc = upload(&m->d_lut, d->lut, bytes))) {
+  const size_t nval = (size_t)d->lut_rows * d->lut_cols * 4, bytes = nval * 4;
+  auto rounded = [&](const float* src) {  // every value rounded to FP16 (round to nearest even)
+    std::vector<float> r(nval);
+    for (size_t i = 0; i < nval; i++) r[i] = __half2float(__float2half_rn(src[i]));
+    return r;
+  };
+  const std::vector<float> lut16 = rounded(d->lut);
+  if ((rc = upload(&m->d_lut, d->lut, bytes)) || (rc = upload(&m->d_lut16, lut16.data(), bytes))) {
     pz_model_destroy(m);
     return rc;
   }
-  if (d->lut_ar && (rc = upload(&m->d_lut_ar, d->lut_ar, bytes))) {
-    pz_model_destroy(m);
-    return rc;
+  if (d->lut_ar) {
+    const std::vector<float> ar16 = rounded(d->lut_ar);
+    if ((rc = upload(&m->d_lut_ar, d->lut_ar, bytes)) || (rc = upload(&m->d_lut_ar16, ar16.data(), bytes))) {
+      pz_model_destroy(m);
+      return rc;
+    }
   }
   *out = m;
   return PZ_OK;
@@ -287,6 +296,8 @@ void pz_model_destroy(pz_model* m) {
   if (!m) return;
   cudaFree(m->d_lut);
   cudaFree(m->d_lut_ar);
+  cudaFree(m->d_lut16);
+  cudaFree(m->d_lut_ar16);
   cudaFree(m->d_wts);
   cudaFree(m->d_cs);
   cudaFree(m->d_bias);
@@ -322,6 +333,10 @@ int pz_run(const pz_model* m, const pz_plane* in, int n_in, pz_plane* out, int n
       return fail(PZ_EINVAL, "output planes differ in size");
   }
   const int W = in[0].width, H = in[0].height, dt = in[0].dtype;
+  if (o && (o->precision < PZ_PREC_FP32 || o->precision > PZ_PREC_MPV))
+    return fail(PZ_EINVAL, "unknown precision %d", o->precision);
+  if (o && o->precision == PZ_PREC_MPV && dt != PZ_F16)
+    return fail(PZ_EINVAL, "the mpv form takes FP16 planes (the host's textures are rgba16f)");
   int OW = 2 * W, OH = 2 * H;
   if (m->family == PZ_RAVU_3X) {
     OW = 3 * W;
@@ -396,10 +411,7 @@ int pz_run(const pz_model* m, const pz_plane* in, int n_in, pz_plane* out, int n
     a.H = H;
     a.OW = OW;
     a.OH = OH;
-    a.lut = m->d_lut;
-    a.lut_ar = m->d_lut_ar;
-    a.lut_rows = m->lut_rows;
-    a.lut_cols = m->lut_cols;
+    pz::select_lut(m, o ? o->precision : PZ_PREC_FP32, &a);
     a.ar = m->ar;
     a.keys = o ? o->keys : nullptr;
     a.err = pz::device_error_word();

@@ -86,10 +86,7 @@ int build_tables(const pz_job* jobs, int n, std::vector<pz::DevJob>* table, pz_b
         a.H = j.in[0].height;
         a.OW = j.out[0].width;
         a.OH = j.out[0].height;
-        a.lut = m->d_lut;
-        a.lut_ar = m->d_lut_ar;
-        a.lut_rows = m->lut_rows;
-        a.lut_cols = m->lut_cols;
+        pz::select_lut(m, j.opts.precision, &a);
         a.ar = m->ar;
         a.keys = nullptr;
         a.err = pz::device_error_word();
@@ -128,6 +125,10 @@ int validate_job(const pz_job& j, int idx) {
         o.height != j.out[0].height)
       return pz::set_error(PZ_EINVAL, "job %d: planes differ in size", idx);
   }
+  if (j.opts.precision < PZ_PREC_FP32 || j.opts.precision > PZ_PREC_MPV)
+    return pz::set_error(PZ_EINVAL, "job %d: unknown precision %d", idx, j.opts.precision);
+  if (j.opts.precision == PZ_PREC_MPV && j.in[0].dtype != PZ_F16)
+    return pz::set_error(PZ_EINVAL, "job %d: the mpv form takes FP16 planes", idx);
   const int W = j.in[0].width, H = j.in[0].height, OW = j.out[0].width, OH = j.out[0].height;
   const size_t es = j.in[0].dtype == PZ_F32 ? 4 : 2;
   switch (m->family) {

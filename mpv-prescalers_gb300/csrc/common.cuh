@@ -135,20 +135,16 @@ __device__ __forceinline__ int ravu_key(float a, float b, float d, const KeyPara
   return (int)((angle * (float)kp.n_strength + strength) * 3.0f + coherence);
 }
 
-// Anti-ringing powers: (0.1+v)^32, ^33 and (1.1-v)^32, ^33 by 5 squarings
-// (ravu-lite-ar-r3.hook:91-98).
-struct ArPow {
-  float h32, h33, l32, l33;
-};
-__device__ __forceinline__ ArPow ar_pow(float v) {
-  float h = 0.1f + v, l = 1.1f - v;
-  float h32 = h, l32 = l;
+// Anti-ringing powers of one value as FP32x2 pairs: (h^32, l^32) and
+// (h^33, l^33) with h = 0.1 + v, l = 1.1 - v, pow(x, 32) by five squarings
+// (ravu-lite-ar-r3.hook:91-98); each lane rounds as a scalar FMUL would.
+__device__ __forceinline__ void ar_pow2(float v, float2& p32, float2& p33) {
+  const float2 hl = __ffma2_rn(make_float2(v, v), make_float2(1.0f, -1.0f), make_float2(0.1f, 1.1f));
+  float2 q = hl;
 #pragma unroll
-  for (int i = 0; i < 5; i++) {
-    h32 *= h32;
-    l32 *= l32;
-  }
-  return {h32, h32 * h, l32, l32 * l};
+  for (int i = 0; i < 5; i++) q = __fmul2_rn(q, q);
+  p32 = q;
+  p33 = __fmul2_rn(q, hl);
 }
 
 // lo = 1.1 - lo2/lo; hi = hi2/hi - 0.1; mix(res, clamp(res, lo, hi), s)

@@ -25,6 +25,7 @@ struct RavuArgs {
   int32_t* keys;     // optional raw-key output
   int* err;          // device error word (kErr*)
   int staging;       // 0: clamped loads, 1: TMA boxes for interior tiles
+  float lut_frac;    // zoom LUT bilinear fraction steps (0: exact FP32)
   KeyParams kp;
 };
 

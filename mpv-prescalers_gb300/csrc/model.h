@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_fp16.h>
 
+#include "../../include/prescale.h"
 #include "kernels.h"
 
 struct pz_model {
@@ -10,6 +11,8 @@ struct pz_model {
   float ar = 0.0f;
   float4* d_lut = nullptr;
   float4* d_lut_ar = nullptr;
+  float4* d_lut16 = nullptr;     // the LUTs with every value rounded to FP16
+  float4* d_lut_ar16 = nullptr;
   int lut_rows = 0, lut_cols = 0;
   pz::KeyParams kp{};
   int nns = 0, win_w = 0, win_h = 0;
@@ -23,4 +26,15 @@ struct pz_model {
 namespace pz {
 // Record `msg` for pz_last_error() on the calling thread; returns `code`.
 int set_error(int code, const char* fmt, ...);
+
+// The LUTs and LUT sampling of a precision form: the mpv form reads the
+// FP16-rounded copies and quantises zoom bilinear fractions to 1/256.
+inline void select_lut(const pz_model* m, int precision, RavuArgs* a) {
+  const bool mpv = precision == PZ_PREC_MPV;
+  a->lut = mpv ? m->d_lut16 : m->d_lut;
+  a->lut_ar = mpv ? m->d_lut_ar16 : m->d_lut_ar;
+  a->lut_rows = m->lut_rows;
+  a->lut_cols = m->lut_cols;
+  a->lut_frac = mpv ? 256.0f : 0.0f;
+}
 }  // namespace pz

@@ -126,6 +126,7 @@ __device__ __forceinline__ bool stage_frame(const RavuArgs& p, const TmaCtx* t, 
   return r >= 0;
 }
 
+
 // ------------------------------------------------------------ ravu-lite ---
 // Does lite LUT column c take part in the anti-ringing sums?  r2: every
 // tap; r3/r4: the 13-tap diamond |dx|+|dy| <= 2 (ravu-lite-ar-r3.hook:93-170).
@@ -139,74 +140,79 @@ struct LiteTile {
   static constexpr int N = 2 * R - 1, S = N * N, HALO = R - 1;
   static constexpr int TW = kTileW + N - 1, TH = kTileH + N - 1;
   // value tile, then (AR) the anti-ringing powers of every tile value
-  static constexpr size_t smem_bytes = (size_t)((TW * TH + 3) & ~3) * 4 + (AR ? (size_t)TW * TH * 16 : 0);
+  static constexpr size_t smem_bytes = (size_t)((TW * TH + 3) & ~3) * 4;
 
   static constexpr int kPlanes = 1;
   using Elem = T;
 
   __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, const TmaCtx* tma = nullptr) {
     float* tile = smem;
-    float4* ptile = reinterpret_cast<float4*>(smem + ((TW * TH + 3) & ~3));
     if (!stage_frame<kLuma, TW, TH, T>(p, tma, x0 - HALO, y0 - HALO, tile, nullptr)) return;
     __syncthreads();
-    if (AR) {  // (h32, l32, h33, l33) once per value instead of once per window tap
-      for (int i = threadIdx.x; i < TW * TH; i += kTileThreads) {
-        const ArPow q = ar_pow(tile[i]);
-        ptile[i] = make_float4(q.h32, q.l32, q.h33, q.l33);
-      }
-      __syncthreads();
-    }
     const int tx = threadIdx.x % kTileW, ty = threadIdx.x / kTileW;
     const int gx = x0 + tx, gy = y0 + ty;
     if (gx >= p.W || gy >= p.H) return;
     auto get = [&](int kx, int ky) { return tile[(ty + ky) * TW + tx + kx]; };
-    auto pw = [&](int k) {
-      const float4 q = ptile[(ty + k % N) * TW + tx + k / N];
-      return ArPow{q.x, q.z, q.y, q.w};
-    };
     float a, b, d;
     structure_tensor<N, false>(get, p.kp, a, b, d);
     const int key = ravu_key(a, b, d, p.kp);
     if (p.keys) p.keys[(size_t)gy * p.W + gx] = key;
     const float4* L = p.lut + (size_t)min(max(key, 0), p.lut_rows - 1) * p.lut_cols;
-    float4 res = make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 hi = res, lo = res, hi2 = res, lo2 = res;
+    // FP32x2 sums: P = sum va*w, Q = sum vb*w, res = P + Q.wzyx; the
+    // anti-ringing sums of output k as (hi, lo) and (hi2, lo2) pairs
+    float2 P01 = make_float2(0.f, 0.f), P23 = P01, Q01 = P01, Q23 = P01;
+    float2 HL[4], HL3[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) HL[k] = HL3[k] = P01;
 #pragma unroll
     for (int c = 0; c < S / 2; c++) {
       const float4 w = __ldg(L + c);
       const float va = get(c / N, c % N), vb = get((S - 1 - c) / N, (S - 1 - c) % N);
-      // res += va * w + vb * w.wzyx
-      res.x += va * w.x + vb * w.w;
-      res.y += va * w.y + vb * w.z;
-      res.z += va * w.z + vb * w.y;
-      res.w += va * w.w + vb * w.x;
+      const float2 w01 = make_float2(w.x, w.y), w23 = make_float2(w.z, w.w);
+      const float2 a2 = make_float2(va, va), b2 = make_float2(vb, vb);
+      P01 = __ffma2_rn(a2, w01, P01);
+      P23 = __ffma2_rn(a2, w23, P23);
+      Q01 = __ffma2_rn(b2, w01, Q01);
+      Q23 = __ffma2_rn(b2, w23, Q23);
       if (AR && lite_ar_col<R>(c)) {
-        const float4 wg = make_float4(fmaxf(w.x, 0.f), fmaxf(w.y, 0.f), fmaxf(w.z, 0.f), fmaxf(w.w, 0.f));
-        const ArPow pa = pw(c), pb = pw(S - 1 - c);
-        hi.x += pa.h32 * wg.x + pb.h32 * wg.w;  hi.y += pa.h32 * wg.y + pb.h32 * wg.z;
-        hi.z += pa.h32 * wg.z + pb.h32 * wg.y;  hi.w += pa.h32 * wg.w + pb.h32 * wg.x;
-        lo.x += pa.l32 * wg.x + pb.l32 * wg.w;  lo.y += pa.l32 * wg.y + pb.l32 * wg.z;
-        lo.z += pa.l32 * wg.z + pb.l32 * wg.y;  lo.w += pa.l32 * wg.w + pb.l32 * wg.x;
-        hi2.x += pa.h33 * wg.x + pb.h33 * wg.w; hi2.y += pa.h33 * wg.y + pb.h33 * wg.z;
-        hi2.z += pa.h33 * wg.z + pb.h33 * wg.y; hi2.w += pa.h33 * wg.w + pb.h33 * wg.x;
-        lo2.x += pa.l33 * wg.x + pb.l33 * wg.w; lo2.y += pa.l33 * wg.y + pb.l33 * wg.z;
-        lo2.z += pa.l33 * wg.z + pb.l33 * wg.y; lo2.w += pa.l33 * wg.w + pb.l33 * wg.x;
+        const float g[4] = {fmaxf(w.x, 0.f), fmaxf(w.y, 0.f), fmaxf(w.z, 0.f), fmaxf(w.w, 0.f)};
+        float2 ha, ha3, hb, hb3;
+        ar_pow2(va, ha, ha3);
+        ar_pow2(vb, hb, hb3);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          const float2 gk = make_float2(g[k], g[k]), gr = make_float2(g[3 - k], g[3 - k]);
+          HL[k] = __ffma2_rn(ha, gk, HL[k]);
+          HL[k] = __ffma2_rn(hb, gr, HL[k]);
+          HL3[k] = __ffma2_rn(ha3, gk, HL3[k]);
+          HL3[k] = __ffma2_rn(hb3, gr, HL3[k]);
+        }
       }
     }
     {
       constexpr int c = S / 2;
       const float4 w = __ldg(L + c);
       const float v = get(c / N, c % N);
-      res.x += v * w.x; res.y += v * w.y; res.z += v * w.z; res.w += v * w.w;
+      const float2 v2 = make_float2(v, v);
+      P01 = __ffma2_rn(v2, make_float2(w.x, w.y), P01);
+      P23 = __ffma2_rn(v2, make_float2(w.z, w.w), P23);
       if (AR) {
-        const float4 wg = make_float4(fmaxf(w.x, 0.f), fmaxf(w.y, 0.f), fmaxf(w.z, 0.f), fmaxf(w.w, 0.f));
-        const ArPow pc = pw(c);
-        hi.x += pc.h32 * wg.x; hi.y += pc.h32 * wg.y; hi.z += pc.h32 * wg.z; hi.w += pc.h32 * wg.w;
-        lo.x += pc.l32 * wg.x; lo.y += pc.l32 * wg.y; lo.z += pc.l32 * wg.z; lo.w += pc.l32 * wg.w;
-        hi2.x += pc.h33 * wg.x; hi2.y += pc.h33 * wg.y; hi2.z += pc.h33 * wg.z; hi2.w += pc.h33 * wg.w;
-        lo2.x += pc.l33 * wg.x; lo2.y += pc.l33 * wg.y; lo2.z += pc.l33 * wg.z; lo2.w += pc.l33 * wg.w;
+        const float g[4] = {fmaxf(w.x, 0.f), fmaxf(w.y, 0.f), fmaxf(w.z, 0.f), fmaxf(w.w, 0.f)};
+        float2 hc, hc3;
+        ar_pow2(v, hc, hc3);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          const float2 gk = make_float2(g[k], g[k]);
+          HL[k] = __ffma2_rn(hc, gk, HL[k]);
+          HL3[k] = __ffma2_rn(hc3, gk, HL3[k]);
+        }
       }
     }
+    float4 res = make_float4(P01.x + Q23.y, P01.y + Q23.x, P23.x + Q01.y, P23.y + Q01.x);
+    const float4 hi = make_float4(HL[0].x, HL[1].x, HL[2].x, HL[3].x);
+    const float4 lo = make_float4(HL[0].y, HL[1].y, HL[2].y, HL[3].y);
+    const float4 hi2 = make_float4(HL3[0].x, HL3[1].x, HL3[2].x, HL3[3].x);
+    const float4 lo2 = make_float4(HL3[0].y, HL3[1].y, HL3[2].y, HL3[3].y);
     if (AR) {  // no [0,1] clamp after anti-ringing (compute/ravu-lite-ar-r3.hook:166)
       res.x = ar_finish(res.x, lo.x, hi.x, lo2.x, hi2.x, p.ar);
       res.y = ar_finish(res.y, lo.y, hi.y, lo2.y, hi2.y, p.ar);
@@ -468,11 +474,17 @@ __device__ __forceinline__ ZoomPos zoom_pos(int X, int W, int OW) {
 // Bilinear (FILTER LINEAR) fetch of one LUT texel at block column `blk` and
 // sub-position (sx, sy) of key block `key`: x = blk*9 + 8 sx, y = key*9 + 8 sy
 // (LUTPOS(x, 9) / (blocks, 288), ravu-zoom-r2.hook:23-31); clamp-to-edge.
+// With q > 0 the fractions are rounded to multiples of 1/q, as a texture
+// unit's fixed-point filter weights are (q = 256: 8 fractional bits).
 __device__ __forceinline__ float4 lut_bilinear(const float4* lut, int rows, int cols, int key, int blk, float sx,
-                                               float sy) {
+                                               float sy, float q) {
   const float fx8 = 8.0f * sx, fy8 = 8.0f * sy;
   const float x0f = floorf(fx8), y0f = floorf(fy8);
-  const float fx = fx8 - x0f, fy = fy8 - y0f;
+  float fx = fx8 - x0f, fy = fy8 - y0f;
+  if (q > 0.0f) {
+    fx = rintf(fx * q) / q;
+    fy = rintf(fy * q) / q;
+  }
   const int xa = min(blk * 9 + (int)x0f, cols - 1), xb = min(xa + 1, cols - 1);
   const int ya = clampi(key * 9 + (int)y0f, 0, rows - 1), yb = min(ya + 1, rows - 1);
   const float4 v00 = __ldg(lut + (size_t)ya * cols + xa), v01 = __ldg(lut + (size_t)ya * cols + xb);
@@ -538,17 +550,22 @@ struct ZoomTile {
     const int key = ravu_key(a, b, d, p.kp);  // no +0.5 row centring (ravu-zoom-r2.hook:124)
     if (p.keys) p.keys[(size_t)Y * p.OW + X] = key;
     const float sx = px.s, sy = py.s, ix = 1.0f - sx, iy = 1.0f - sy;
-    float res[C], hi[C], lo[C], hi2[C], lo2[C];
+    // anti-ringing sums per channel as FP32x2 pairs (hi, lo) and (hi2, lo2)
+    float res[C];
+    float2 HL[C], HL3[C];
 #pragma unroll
-    for (int c = 0; c < C; c++) res[c] = hi[c] = lo[c] = hi2[c] = lo2[c] = 0.0f;
+    for (int c = 0; c < C; c++) {
+      res[c] = 0.0f;
+      HL[c] = HL3[c] = make_float2(0.0f, 0.0f);
+    }
 #pragma unroll
     for (int blk = 0; blk < NB; blk++) {
-      const float4 ws = lut_bilinear(p.lut, p.lut_rows, p.lut_cols, key, blk, sx, sy);
-      const float4 wi = lut_bilinear(p.lut, p.lut_rows, p.lut_cols, key, blk, ix, iy);
+      const float4 ws = lut_bilinear(p.lut, p.lut_rows, p.lut_cols, key, blk, sx, sy, p.lut_frac);
+      const float4 wi = lut_bilinear(p.lut, p.lut_rows, p.lut_cols, key, blk, ix, iy, p.lut_frac);
       float4 as = make_float4(0.f, 0.f, 0.f, 0.f), ai = as;
       if (AR) {
-        as = lut_bilinear(p.lut_ar, p.lut_rows, p.lut_cols, key, blk, sx, sy);
-        ai = lut_bilinear(p.lut_ar, p.lut_rows, p.lut_cols, key, blk, ix, iy);
+        as = lut_bilinear(p.lut_ar, p.lut_rows, p.lut_cols, key, blk, sx, sy, p.lut_frac);
+        ai = lut_bilinear(p.lut_ar, p.lut_rows, p.lut_cols, key, blk, ix, iy, p.lut_frac);
       }
 #pragma unroll
       for (int j = 0; j < 4; j++) {
@@ -561,12 +578,15 @@ struct ZoomTile {
             res[c] += va * comp4(ws, j);
             res[c] += vb * comp4(wi, j);
             if (AR) {
-              const ArPow pa = ar_pow(va), pb = ar_pow(vb);
-              const float wa = comp4(as, j), wb = comp4(ai, j);
-              hi[c] += pa.h32 * wa + pb.h32 * wb;
-              lo[c] += pa.l32 * wa + pb.l32 * wb;
-              hi2[c] += pa.h33 * wa + pb.h33 * wb;
-              lo2[c] += pa.l33 * wa + pb.l33 * wb;
+              float2 pa, pa3, pb, pb3;
+              ar_pow2(va, pa, pa3);
+              ar_pow2(vb, pb, pb3);
+              const float2 wa = make_float2(comp4(as, j), comp4(as, j));
+              const float2 wb = make_float2(comp4(ai, j), comp4(ai, j));
+              HL[c] = __ffma2_rn(pa, wa, HL[c]);
+              HL[c] = __ffma2_rn(pb, wb, HL[c]);
+              HL3[c] = __ffma2_rn(pa3, wa, HL3[c]);
+              HL3[c] = __ffma2_rn(pb3, wb, HL3[c]);
             }
           }
         }
@@ -574,7 +594,7 @@ struct ZoomTile {
     }
 #pragma unroll
     for (int c = 0; c < C; c++) {
-      const float v = AR ? ar_finish(res[c], lo[c], hi[c], lo2[c], hi2[c], p.ar) : clampf(res[c], 0.f, 1.f);
+      const float v = AR ? ar_finish(res[c], HL[c].y, HL[c].x, HL3[c].y, HL3[c].x, p.ar) : clampf(res[c], 0.f, 1.f);
       stp(static_cast<T*>(p.out[c]) + (size_t)Y * p.out_pitch[c] + X, v);
     }
   }

@@ -36,7 +36,7 @@ PlaneLike = Union["torch.Tensor", Sequence["torch.Tensor"]]
 _FAMILY_CODE = {"lite": _ffi.PZ_RAVU_LITE, "ravu": _ffi.PZ_RAVU, "zoom": _ffi.PZ_RAVU_ZOOM,
                 "3x": _ffi.PZ_RAVU_3X, "nnedi3": _ffi.PZ_NNEDI3}
 _CHANNEL_CODE = {"luma": _ffi.PZ_LUMA, "yuv": _ffi.PZ_YUV, "rgb": _ffi.PZ_RGB}
-PRECISIONS = {"fp32": _ffi.PZ_PREC_FP32, "fast": _ffi.PZ_PREC_FAST}
+PRECISIONS = {"fp32": _ffi.PZ_PREC_FP32, "fast": _ffi.PZ_PREC_FAST, "mpv": _ffi.PZ_PREC_MPV}
 # RAVU halo staging: clamped loads, or TMA boxes for interior tiles
 STAGINGS = {"ldg": 0, "tma": 1}
 
@@ -86,6 +86,44 @@ class HookModel:
         if fam == "zoom":
             return "ALIGN"
         return (0.0, 0.0)
+
+    @property
+    def hook_point(self) -> str:
+        """The texture the chain hooks: LUMA (luma files), NATIVE (yuv:
+        merged planes before RGB conversion) or MAIN (rgb); e.g.
+        ``ravu-lite-r3.hook:16``, ``compute/ravu-r2-yuv.hook:15``,
+        ``ravu-r2-rgb.hook:16``."""
+        return self.passes[0].hooks[0] if self.passes and self.passes[0].hooks else "LUMA"
+
+    def chain_offset(self, in_w: int, in_h: int, out_size: Optional[Tuple[int, int]] = None,
+                     luma_w: Optional[int] = None):
+        """Pixel shift of the chain's output that the host would correct in
+        its next scaling pass: the sum of the ``//!OFFSET`` of every enabled
+        pass that replaces the hooked texture, in output pixels (ravu
+        ``(-0.5, -0.5)``; nnedi3 ``(0, -0.5)`` per doubled row axis and
+        ``(-0.5, 0)`` per doubled column axis; lite and 3x none).
+        ``"ALIGN"`` when the chain aligns centres itself (ravu-zoom)."""
+        if not self.enabled(in_w, in_h, out_size, luma_w=luma_w):
+            return (0.0, 0.0)
+        if self.family == "nnedi3":
+            ax = self.nnedi3_axes(in_w, in_h, out_size)
+            ox = oy = 0.0
+            for p in self.passes:
+                if p.save is None and isinstance(p.offset, tuple):
+                    y_pass = "_y" in p.desc
+                    if (y_pass and ax & 1) or (not y_pass and ax & 2):
+                        ox += p.offset[0]
+                        oy += p.offset[1]
+            return (ox, oy)
+        ox = oy = 0.0
+        for p in self.passes:
+            if p.save is not None or p.offset is None:
+                continue
+            if p.offset == "ALIGN":
+                return "ALIGN"
+            ox += p.offset[0]
+            oy += p.offset[1]
+        return (ox, oy)
 
     def __repr__(self):
         return f"HookModel({self.name!r}, family={self.family!r}, channels={self.channels!r})"
@@ -188,7 +226,10 @@ class HookModel:
                     ax |= 2
         return ax
 
-    def enabled(self, in_w: int, in_h: int, out_size: Optional[Tuple[int, int]] = None) -> bool:
+    def enabled(self, in_w: int, in_h: int, out_size: Optional[Tuple[int, int]] = None,
+                luma_w: Optional[int] = None) -> bool:
+        """The chain's ``//!WHEN`` for this size; ``luma_w`` is the width of
+        the frame's luma plane (0 for RGB frames, which have none)."""
         if self.family == "nnedi3":
             return self.nnedi3_axes(in_w, in_h, out_size) != 0
         if out_size is None:
@@ -196,7 +237,8 @@ class HookModel:
             if s is None:
                 raise ValueError("ravu-zoom needs out_size=(width, height)")
             out_size = (s * in_w, s * in_h)
-        return _models.pass_enabled(self.passes[0], in_w, in_h, out_size[0], out_size[1], luma_w=in_w)
+        return _models.pass_enabled(self.passes[0], in_w, in_h, out_size[0], out_size[1],
+                                    luma_w=in_w if luma_w is None else luma_w)
 
     # ---- execution ----------------------------------------------------
     def upscale(self, planes: PlaneLike, out_size: Optional[Tuple[int, int]] = None, precision: str = "fp32",
@@ -208,8 +250,11 @@ class HookModel:
         ``[H][W]`` tensors.
         ``out_size``: target ``(width, height)``; required for ravu-zoom,
         otherwise it only decides the ``//!WHEN`` conditions.
-        ``precision``: "fp32" (plain FP32 arithmetic) or "fast" (FP16
-        tensor-core NNEDI3 neurons; RAVU arithmetic stays FP32).
+        ``precision``: "fp32" (plain FP32 arithmetic), "fast" (FP16
+        tensor-core NNEDI3 neurons; RAVU arithmetic stays FP32) or "mpv"
+        (what the mpv host computes, to measure the distance to it: FP16
+        planes only, LUTs rounded to FP16, ravu-zoom LUT bilinear weights
+        in 1/256 steps; NNEDI3 as "fp32").
         ``staging``: how RAVU tiles stage their input window: "ldg"
         (clamped loads) or "tma" (TMA boxes for interior tiles); the pixels
         are identical, only the speed differs (see ``batch.autotune_staging``).

@@ -133,9 +133,16 @@ def synthetic_model(name: str, seed: int = 0):
     info = _parse_name(name)
     rng = np.random.default_rng(seed + sum(map(ord, name)))
 
-    def mkpass(desc, when, save=None):
-        return Pass(desc=desc, hooks=["LUMA"], binds=["HOOKED"], save=save, width=None, height=None,
-                    offset=None, when=when, components=None, compute=None, body=[], line=0, body_line=0)
+    # hook point and //!OFFSET as in the real files: luma files hook LUMA,
+    # yuv NATIVE, rgb MAIN (compute/ravu-r2-yuv.hook:15, ravu-r2-rgb.hook:16);
+    # ravu ends with OFFSET -0.5 -0.5 (ravu-r3.hook:424), zoom with ALIGN
+    # (ravu-zoom-r2.hook:21), the NNEDI3 combine passes with 0 -0.5 and
+    # -0.5 0 (nnedi3-nns16-win8x4.hook:95,185)
+    hook = {"luma": "LUMA", "yuv": "NATIVE", "rgb": "MAIN"}[info.get("channels", "luma")]
+
+    def mkpass(desc, when, save=None, offset=None, width=None, height=None):
+        return Pass(desc=desc, hooks=[hook], binds=["HOOKED"], save=save, width=width, height=height,
+                    offset=offset, when=when, components=None, compute=None, body=[], line=0, body_line=0)
 
     if info["family"] == "nnedi3":
         nns, wh = info["nns"], info["win_h"]
@@ -145,9 +152,11 @@ def synthetic_model(name: str, seed: int = 0):
         A -= A.mean(0)
         B -= B.mean(0)
         passes = [mkpass(f"NNEDI3 (double_y, nns{nns}, win8x{wh})", "HOOKED.h OUTPUT.h / 0.707106 <", "nnedi3_int"),
-                  mkpass(f"NNEDI3 (combine_y, nns{nns}, win8x{wh})", "HOOKED.h OUTPUT.h / 0.707106 <"),
+                  mkpass(f"NNEDI3 (combine_y, nns{nns}, win8x{wh})", "HOOKED.h OUTPUT.h / 0.707106 <",
+                         offset=(0.0, -0.5), height="2 HOOKED.h *"),
                   mkpass(f"NNEDI3 (double_x, nns{nns}, win8x{wh})", "HOOKED.w OUTPUT.w / 0.707106 <", "nnedi3_int"),
-                  mkpass(f"NNEDI3 (combine_x, nns{nns}, win8x{wh})", "HOOKED.w OUTPUT.w / 0.707106 <")]
+                  mkpass(f"NNEDI3 (combine_x, nns{nns}, win8x{wh})", "HOOKED.w OUTPUT.w / 0.707106 <",
+                         offset=(-0.5, 0.0), width="2 HOOKED.w *")]
         return Nnedi3Model(name=name, nns=nns, win_w=8, win_h=wh,
                            taps=np.asarray(geo.nnedi3_taps(8, wh), dtype=np.int32),
                            weights_a=A.astype(np.float32), weights_b=B.astype(np.float32),
@@ -192,7 +201,12 @@ def synthetic_model(name: str, seed: int = 0):
     if fam == "zoom" and info["ar"]:
         lut_ar = (rng.random(lut.shape) * 0.1).astype(np.float32)
     when = _WHEN_ZOOM if fam == "zoom" else (_WHEN_3X if fam == "3x" else _WHEN_2X)
-    passes = [mkpass(f"synthetic {name}", when)]
+    if info["channels"] == "yuv":
+        when += " LUMA.w 0 > *"   # yuv files need a luma plane (compute/ravu-r2-yuv.hook:19)
+    scale = {"zoom": None, "3x": "3"}.get(fam, "2")
+    passes = [mkpass(f"synthetic {name}", when, offset={"ravu": (-0.5, -0.5), "zoom": "ALIGN"}.get(fam),
+                     width=f"{scale} HOOKED.w *" if scale else "OUTPUT.w",
+                     height=f"{scale} HOOKED.h *" if scale else "OUTPUT.h")]
     return RavuModel(name=name, family=fam, radius=r, channels=info["channels"], ar=info["ar"], lut=lut,
                      lut_ar=lut_ar, grad_weights=np.asarray(geo.grad_weights(fam, r)), strength=strength,
                      coherence=(0.25, 0.5), passes=passes, style="synthetic", path="<synthetic>",

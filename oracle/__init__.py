@@ -16,5 +16,5 @@ against the GLSL shim in ``oracle/glsl_shim.hpp``; ``tests/golden/`` holds
 input/output vectors produced by that build, and ``tests/test_oracle.py``
 checks this restatement against them.
 """
-from .ravu import ravu_lite, ravu_3x, ravu_lattice, ravu_zoom, keyed_upscale  # noqa: F401
+from .ravu import ravu_lite, ravu_3x, ravu_lattice, ravu_zoom, keyed_upscale, mpv_form  # noqa: F401
 from .nnedi3 import nnedi3_double, nnedi3_upscale  # noqa: F401

@@ -374,13 +374,18 @@ def ravu_lattice(model, planes, keys: Optional[np.ndarray] = None, int11: Option
 
 # ----------------------------------------------------------- ravu-zoom ----
 
-def _bilinear(lut: np.ndarray, tx: np.ndarray, ty: np.ndarray, comp: int) -> np.ndarray:
-    """FILTER LINEAR fetch of one component at texel coordinates (centre = k)."""
+def _bilinear(lut: np.ndarray, tx: np.ndarray, ty: np.ndarray, comp: int, frac_steps=None) -> np.ndarray:
+    """FILTER LINEAR fetch of one component at texel coordinates (centre = k);
+    ``frac_steps`` rounds the fractions to multiples of 1/frac_steps, as a
+    texture unit's fixed-point weights are (256: 8 fractional bits)."""
     h, w = lut.shape[:2]
     x0 = np.floor(tx)
     y0 = np.floor(ty)
     fx = tx - x0
     fy = ty - y0
+    if frac_steps:
+        fx = np.rint(fx * frac_steps) / frac_steps
+        fy = np.rint(fy * frac_steps) / frac_steps
     x0 = x0.astype(np.int64)
     y0 = y0.astype(np.int64)
     xa = np.clip(x0, 0, w - 1); xb = np.clip(x0 + 1, 0, w - 1)
@@ -390,7 +395,7 @@ def _bilinear(lut: np.ndarray, tx: np.ndarray, ty: np.ndarray, comp: int) -> np.
     return (v00 * (1 - fx) + v01 * fx) * (1 - fy) + (v10 * (1 - fx) + v11 * fx) * fy
 
 
-def ravu_zoom(model, planes, out_w: int, out_h: int, keys: Optional[np.ndarray] = None):
+def ravu_zoom(model, planes, out_w: int, out_h: int, keys: Optional[np.ndarray] = None, frac_steps=None):
     """Arbitrary-ratio ravu-zoom(-ar) (``ravu-zoom-r2.hook:24-138``).
 
     Output pixel (X, Y) samples the input around
@@ -429,12 +434,12 @@ def ravu_zoom(model, planes, out_w: int, out_h: int, keys: Optional[np.ndarray] 
         lo2 = np.zeros_like(res); hi2 = np.zeros_like(res)
     for i in range(S // 2):
         blk, comp = i // 4, i % 4
-        w_sub = _bilinear(lut, blk * 9.0 + 8.0 * spx, ty_sub, comp)
-        w_inv = _bilinear(lut, blk * 9.0 + 8.0 * (1.0 - spx), ty_inv, comp)
+        w_sub = _bilinear(lut, blk * 9.0 + 8.0 * spx, ty_sub, comp, frac_steps)
+        w_inv = _bilinear(lut, blk * 9.0 + 8.0 * (1.0 - spx), ty_inv, comp, frac_steps)
         res += vals[i] * w_sub + vals[S - 1 - i] * w_inv
         if ar:
-            a_sub = _bilinear(lut_ar, blk * 9.0 + 8.0 * spx, ty_sub, comp)
-            a_inv = _bilinear(lut_ar, blk * 9.0 + 8.0 * (1.0 - spx), ty_inv, comp)
+            a_sub = _bilinear(lut_ar, blk * 9.0 + 8.0 * spx, ty_sub, comp, frac_steps)
+            a_inv = _bilinear(lut_ar, blk * 9.0 + 8.0 * (1.0 - spx), ty_inv, comp, frac_steps)
             for v, wa in ((vals[i], a_sub), (vals[S - 1 - i], a_inv)):
                 h1, h2, l1, l2 = _ar_powers(v)
                 hi_s += h1 * wa; lo_s += l1 * wa; hi2 += h2 * wa; lo2 += l2 * wa
@@ -445,9 +450,24 @@ def ravu_zoom(model, planes, out_w: int, out_h: int, keys: Optional[np.ndarray] 
     return res, info
 
 
-def keyed_upscale(model, planes, out_size: Optional[Tuple[int, int]] = None, keys=None, int11=None):
+def mpv_form(model):
+    """The model as the mpv host holds it: every LUT value rounded to FP16
+    (the //!TEXTURE blocks are uploaded as ``//!FORMAT rgba16f``,
+    ``ravu-lite-r3.hook:134``).  Use with ``frac_steps=256`` for ravu-zoom
+    and FP16 planes to restate what the host computes."""
+    import copy
+    m = copy.copy(model)
+    m.lut = np.asarray(model.lut, dtype=np.float32).astype(np.float16).astype(np.float32)
+    if getattr(model, "lut_ar", None) is not None:
+        m.lut_ar = np.asarray(model.lut_ar, dtype=np.float32).astype(np.float16).astype(np.float32)
+    return m
+
+
+def keyed_upscale(model, planes, out_size: Optional[Tuple[int, int]] = None, keys=None, int11=None,
+                  frac_steps=None):
     """Dispatch on the model family; ``out_size`` = (w, h) for ravu-zoom;
-    ``int11`` overrides the int11 plane fed to the ravu lattice passes."""
+    ``int11`` overrides the int11 plane fed to the ravu lattice passes;
+    ``frac_steps`` quantises ravu-zoom's LUT bilinear fractions."""
     fam = model.family
     if fam == "lite":
         return ravu_lite(model, planes, keys)
@@ -458,5 +478,5 @@ def keyed_upscale(model, planes, out_size: Optional[Tuple[int, int]] = None, key
     if fam == "zoom":
         if out_size is None:
             raise ValueError("ravu-zoom needs an output size")
-        return ravu_zoom(model, planes, out_size[0], out_size[1], keys)
+        return ravu_zoom(model, planes, out_size[0], out_size[1], keys, frac_steps)
     raise ValueError(fam)

@@ -53,3 +53,18 @@ def test_struct_layouts_match_the_header(lib):
     # pz_plane: void* + 4 ints
     assert ctypes.sizeof(_ffi.Plane) == 8 + 4 * 4
     assert ctypes.sizeof(_ffi.Opts) >= 4 * 4 + 8 + 8 + 8
+
+
+def test_resample_arguments_are_checked_on_the_host(lib):
+    import ctypes
+    fake = 4096   # never dereferenced: every call below is refused before a launch
+    a = _ffi.Plane(fake, 8, 8, 8, _ffi.PZ_F32)
+    b = _ffi.Plane(fake, 8, 8, 8, _ffi.PZ_F16)
+    assert lib.pz_resample(None, ctypes.byref(a), 1, 0, 1, 0, 0, None) == _ffi.PZ_EINVAL
+    assert lib.pz_resample(ctypes.byref(a), ctypes.byref(b), 1, 0, 1, 0, 0, None) == _ffi.PZ_EINVAL
+    assert b"dtype" in lib.pz_last_error()
+    assert lib.pz_resample(ctypes.byref(a), ctypes.byref(a), 1, 0, 1, 0, 7, None) == _ffi.PZ_EINVAL
+    assert b"filter" in lib.pz_last_error()
+    assert lib.pz_resample(ctypes.byref(a), ctypes.byref(a), float("nan"), 0, 1, 0, 1, None) == _ffi.PZ_EINVAL
+    assert lib.pz_resample(ctypes.byref(a), ctypes.byref(a), 1, 0, 1, 3e9, 1, None) == _ffi.PZ_EINVAL
+    assert b"out of range" in lib.pz_last_error()

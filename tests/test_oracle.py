@@ -83,3 +83,18 @@ def test_planted_oracle_mistake_is_caught(reference_dir):
     finally:
         oracle.ravu._deriv = orig
     assert np.abs(y - g["output"]).max() > 1e-6
+
+
+def test_mpv_form_rounds_luts_to_fp16_and_steps_zoom_fractions():
+    from mpv_prescalers_gb300 import synth
+    m = synth.synthetic_model("ravu-zoom-ar-r2")
+    f = oracle.mpv_form(m)
+    assert np.array_equal(f.lut, m.lut.astype(np.float16).astype(np.float32))
+    assert np.array_equal(f.lut_ar, m.lut_ar.astype(np.float16).astype(np.float32))
+    assert f.lut is not m.lut and m.lut.dtype == np.float32
+    x = synth.luma_plane(12, 14, 3)
+    a, _ = oracle.ravu_zoom(m, x, 25, 21)
+    b, _ = oracle.ravu_zoom(m, x, 25, 21, frac_steps=256)
+    c, _ = oracle.ravu_zoom(m, x, 25, 21, frac_steps=1 << 30)
+    assert 0 < np.abs(a - b).max() < 1e-2      # 1/256 steps move the weights a little
+    assert np.abs(a - c).max() < 1e-7          # ever finer steps converge to exact
