@@ -10,8 +10,8 @@ LUTs of the same shapes (``config.weights`` says which).
 
 Reported (one JSON line on rank 0):
 
-* ``value``: output Mpix/s of the chosen form (FP16 planes, FP32 math), all
-  ranks together, inputs resident in HBM; ``fp32_value``: the plain FP32
+* ``value``: output Mpix/s of the chosen form (FP16 planes, FP16 LUT texels,
+  FP32 math), all ranks together, inputs resident in HBM; ``fp32_value``: the plain FP32
   form (FP32 planes) on the same workload.
 * ``e2e``: the same metric through ``HookModel.upscale`` with the frames
   copied host->device (pinned) and the upscaled frames copied back every step.
@@ -196,27 +196,27 @@ def run_gpu(args):
     stream = torch.cuda.current_stream(dev)
     launches_per_step = NFRAMES * (1 + 2)  # lite: 1 kernel/frame, lattice: 2
 
-    def step(xs, outs, ev=None):
+    def step(xs, outs, prec, ev=None):
         for n in MODELS:
             hm = models[n]
             for f in range(NFRAMES):
                 if ev is not None and n == MODELS[0]:
                     ev.append((torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)))
                     ev[-1][0].record(stream)
-                hm.run_raw([xs[f]], [outs[n][f]], out_size=(2 * W, 2 * H), stream=stream)
+                hm.run_raw([xs[f]], [outs[n][f]], out_size=(2 * W, 2 * H), precision=prec, stream=stream)
                 if ev is not None and n == MODELS[0]:
                     ev[-1][1].record(stream)
 
-    def timed(xs, outs, steps, warmup, kernel_events=None):
+    def timed(xs, outs, prec, steps, warmup, kernel_events=None):
         for _ in range(warmup):
-            step(xs, outs)
+            step(xs, outs, prec)
         torch.cuda.synchronize()
         barrier()
         t0 = torch.cuda.Event(enable_timing=True)
         t1 = torch.cuda.Event(enable_timing=True)
         t0.record(stream)
         for _ in range(steps):
-            step(xs, outs, kernel_events)
+            step(xs, outs, prec, kernel_events)
         t1.record(stream)
         torch.cuda.synchronize()
         barrier()
@@ -225,8 +225,9 @@ def run_gpu(args):
     out_px_step = len(MODELS) * NFRAMES * (2 * W) * (2 * H)
     kev = []
     clk = Clocks(local).__enter__()   # sampled over all three timed loops (device, FP32, end to end)
-    ms16 = timed(x16, outs16, args.steps, args.warmup, kev)
-    ms32 = timed(x32, outs32, args.steps, args.warmup)
+    # chosen form: FP16 planes, FP16 LUT texels (lite), FP32 math; plain form: FP32 everything
+    ms16 = timed(x16, outs16, "fast", args.steps, args.warmup, kev)
+    ms32 = timed(x32, outs32, "fp32", args.steps, args.warmup)
     value = job_value(out_px_step, args.steps, ms16, world)
     fp32_value = job_value(out_px_step, args.steps, ms32, world)
     kern_ms = statistics.mean(a.elapsed_time(b) for a, b in kev)
@@ -239,7 +240,7 @@ def run_gpu(args):
         # public API on host frames: H2D copy, upscale and D2H copy of frame i
         # overlap with its neighbours on three streams
         for n in MODELS:
-            models[n].upscale_host(host_in, out=host_out[n])
+            models[n].upscale_host(host_in, out=host_out[n], precision="fast")
 
     for _ in range(args.warmup):
         e2e_step()
@@ -282,7 +283,8 @@ def run_gpu(args):
             res[prec] = 4 * H * W * reps / (a.elapsed_time(b) / 1e3) / 1e6
         headline[n] = {"chosen_mpix_s": res["fast"], "fp32_mpix_s": res["fp32"],
                        "ratio": res["fast"] / res["fp32"], "chosen": "FP16 planes" + (
-                           ", FP16 tensor-core neurons" if n.startswith("nnedi3") else ", FP32 math")}
+                           ", FP16 tensor-core neurons" if n.startswith("nnedi3") else
+                           ", FP16 LUT texels, FP32 math")}
 
     # ---- serving: Poisson arrivals over 64 streams, mixed resolutions and
     # algorithms (the serving configuration), against serial plain FP32
@@ -319,7 +321,7 @@ def run_gpu(args):
         "metric": "Out Mpix/s 1080p->2160p (ravu-lite-ar-r4 + two-pass ravu-r3, 8 frames each)",
         "value": value, "unit": "Mpix/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms16 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "fp16 planes, fp32 math", "data": "synthetic (seeded sinusoids+polygons+noise)",
+        "dtype": "fp16 planes + fp16 lut texels, fp32 math", "data": "synthetic (seeded sinusoids+polygons+noise)",
         "config": {"workload": "8x 1920x1080 FP16 luma -> 3840x2160 through ravu-lite-ar-r4 and ravu-r3",
                    "frames_per_model": NFRAMES, "weights": {n: sources[n] for n in MODELS},
                    "l2": "per-model working set 166 MB (33 MB in + 133 MB out) > 129 MB L2",
@@ -328,7 +330,7 @@ def run_gpu(args):
         "e2e": {"value": e2e_value, "unit": "Mpix/s",
                 "h2d_bytes_per_step": int(host_in.numel() * host_in.element_size()),
                 "d2h_bytes_per_step": int(sum(t.numel() * t.element_size() for t in host_out.values()))},
-        "roofline": {"bound": "fp32", "kernel": "lite_kernel<4,AR,half> (ravu-lite-ar-r4)",
+        "roofline": {"bound": "fp32", "kernel": "LiteTile<4, AR, half, FP16 texels> (ravu-lite-ar-r4, fast form)",
                      "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s", "frac": achieved_tf / peak_tf,
                      "peak_source": f"{props.multi_processor_count} SMs x 128 FFMA/clk x 2 x {max_mhz:.0f} MHz "
                                     "(FP32 pipe; not in MEASURED_PEAKS.json)",
@@ -390,6 +392,9 @@ CASES = {
     "ravu-r4-yuv": ("ravu-r4-yuv", None, "fp32"),
     "ravu-zoom-ar-r2-rgb": ("ravu-zoom-ar-r2-rgb", (2880, 1620), "fp32"),
     "ravu-3x-r3": ("ravu-3x-r3", None, "fp32"),
+    "ravu-lite-ar-r4-fast": ("ravu-lite-ar-r4", None, "fast"),
+    "ravu-3x-r3-fast": ("ravu-3x-r3", None, "fast"),
+    "ravu-zoom-ar-r2-rgb-fast": ("ravu-zoom-ar-r2-rgb", (2880, 1620), "fast"),
     "nnedi3-nns128-win8x6-fast": ("nnedi3-nns128-win8x6", None, "fast"),
     "nnedi3-nns128-win8x6-fp32": ("nnedi3-nns128-win8x6", None, "fp32"),
 }

@@ -64,7 +64,10 @@ typedef enum { PZ_F32 = 0, PZ_F16 = 1 } pz_dtype;
 
 typedef enum {
   PZ_PREC_FP32 = 0,  /* plain FP32 arithmetic everywhere                    */
-  PZ_PREC_FAST = 1,  /* FP16 tensor-core NNEDI3 neurons; RAVU unchanged     */
+  PZ_PREC_FAST = 1,  /* FP16 tensor-core NNEDI3 neurons; ravu-lite / 3x /
+                        zoom read their LUTs as FP16 texels (half the L1
+                        gather traffic; zoom-ar's anti-ringing LUT stays
+                        FP32), all RAVU arithmetic stays FP32               */
   PZ_PREC_MPV = 2    /* what the mpv host computes, to measure the distance
                         to it: RAVU LUTs rounded to FP16 as the host uploads
                         them (//!FORMAT rgba16f, ravu-lite-r3.hook:134),

@@ -276,8 +276,15 @@ int pz_model_create(const pz_model_desc* d, pz_model** out) {
     for (size_t i = 0; i < nval; i++) r[i] = __half2float(__float2half_rn(src[i]));
     return r;
   };
+  auto halves = [&](const float* src) {  // FP16 texels of the fast form
+    std::vector<__half> r(nval);
+    for (size_t i = 0; i < nval; i++) r[i] = __float2half_rn(src[i]);
+    return r;
+  };
   const std::vector<float> lut16 = rounded(d->lut);
-  if ((rc = upload(&m->d_lut, d->lut, bytes)) || (rc = upload(&m->d_lut16, lut16.data(), bytes))) {
+  const std::vector<__half> luth = halves(d->lut);
+  if ((rc = upload(&m->d_lut, d->lut, bytes)) || (rc = upload(&m->d_lut16, lut16.data(), bytes)) ||
+      (rc = upload(&m->d_lut_h, luth.data(), nval * 2))) {
     pz_model_destroy(m);
     return rc;
   }
@@ -298,6 +305,7 @@ void pz_model_destroy(pz_model* m) {
   cudaFree(m->d_lut_ar);
   cudaFree(m->d_lut16);
   cudaFree(m->d_lut_ar16);
+  cudaFree(m->d_lut_h);
   cudaFree(m->d_wts);
   cudaFree(m->d_cs);
   cudaFree(m->d_bias);

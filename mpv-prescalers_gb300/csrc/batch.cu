@@ -24,13 +24,14 @@
 namespace pz {
 namespace {
 
-int prog_of(const pz_model* m) {
+int prog_of(const pz_model* m, int precision) {
   const int R = m->radius, cm = m->channels, ar = m->ar != 0.0f;
+  const bool h = fast_half_lut(m, precision);
   switch (m->family) {
-    case PZ_RAVU_LITE: return kLite0 + (R - 2) * 2 + ar;
-    case PZ_RAVU_3X: return kThreeX0 + (R - 2) * 3 + cm;
+    case PZ_RAVU_LITE: return (h ? kLiteH0 : kLite0) + (R - 2) * 2 + ar;
+    case PZ_RAVU_3X: return (h ? kThreeXH0 : kThreeX0) + (R - 2) * 3 + cm;
     case PZ_RAVU: return kInt110 + (R - 2) * 3 + cm;
-    case PZ_RAVU_ZOOM: return kZoom0 + (R - 2) * 6 + cm * 2 + ar;
+    case PZ_RAVU_ZOOM: return (h ? kZoomH0 : kZoom0) + (R - 2) * 6 + cm * 2 + ar;
   }
   return -1;
 }
@@ -47,6 +48,7 @@ struct pz_batch {
   struct Group {  // one persistent launch
     int dtype;
     int phase;
+    int hset;       // program set: 1 = the fast form's FP16-texel programs
     int first_job;  // index into the device table
     int n_jobs;
     int total_tiles;
@@ -57,7 +59,7 @@ struct pz_batch {
   void* work = nullptr;
   int n_counters = 0;
   int ctas_per_sm = 0;         // 0 = as many as fit
-  int grid[2] = {0, 0};        // per dtype
+  int grid[2][2] = {{0, 0}, {0, 0}};  // per dtype and program set
 };
 
 namespace {
@@ -66,13 +68,15 @@ int build_tables(const pz_job* jobs, int n, std::vector<pz::DevJob>* table, pz_b
   (void)phase_filter;
   for (int dt = 0; dt < 2; dt++) {
     for (int phase = 0; phase < 2; phase++) {
-      pz_batch::Group g{dt, phase, (int)table->size(), 0, 0, plan->n_counters};
+     for (int hset = 0; hset < 2; hset++) {
+      pz_batch::Group g{dt, phase, hset, (int)table->size(), 0, 0, plan->n_counters};
       for (int i = 0; i < n; i++) {
         const pz_job& j = jobs[i];
         const pz_model* m = j.model;
         if (m->family == PZ_NNEDI3) continue;
         if (j.in[0].dtype != dt) continue;
         if (phase == 1 && m->family != PZ_RAVU) continue;
+        if (pz::fast_half_lut(m, j.opts.precision) != (hset == 1)) continue;
         pz::DevJob d{};
         pz::RavuArgs& a = d.a;
         const int C = m->channels == PZ_LUMA ? 1 : 3;
@@ -91,7 +95,7 @@ int build_tables(const pz_job* jobs, int n, std::vector<pz::DevJob>* table, pz_b
         a.keys = nullptr;
         a.err = pz::device_error_word();
         a.kp = m->kp;
-        d.prog = pz::prog_of(m) + (phase == 1 ? pz::kLattice0 - pz::kInt110 : 0);
+        d.prog = pz::prog_of(m, j.opts.precision) + (phase == 1 ? pz::kLattice0 - pz::kInt110 : 0);
         const bool zoom = m->family == PZ_RAVU_ZOOM;
         const int tw = ((zoom ? a.OW : a.W) + pz::kTileW - 1) / pz::kTileW;
         const int th = ((zoom ? a.OH : a.H) + pz::kTileH - 1) / pz::kTileH;
@@ -105,6 +109,7 @@ int build_tables(const pz_job* jobs, int n, std::vector<pz::DevJob>* table, pz_b
         plan->groups.push_back(g);
         plan->n_counters++;
       }
+     }
     }
   }
   return PZ_OK;
@@ -197,10 +202,13 @@ int pz_batch_create(const pz_job* jobs, int n_jobs, void* work, size_t work_byte
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   for (int dt = 0; dt < 2; dt++) {
-    int fit = dt == 0 ? pz::batch_fit_f32() : pz::batch_fit_f16();
-    if (fit < 1) fit = 1;
-    const int per = ctas_per_sm > 0 ? std::min(ctas_per_sm, fit) : fit;
-    plan->grid[dt] = per * sms;
+    for (int h = 0; h < 2; h++) {
+      int fit = dt == 0 ? (h ? pz::batch_fit_f32h() : pz::batch_fit_f32())
+                        : (h ? pz::batch_fit_f16h() : pz::batch_fit_f16());
+      if (fit < 1) fit = 1;
+      const int per = ctas_per_sm > 0 ? std::min(ctas_per_sm, fit) : fit;
+      plan->grid[dt][h] = per * sms;
+    }
   }
   *out = plan;
   return PZ_OK;
@@ -217,11 +225,10 @@ int pz_batch_launch(const pz_batch* plan, void* stream) {
     if (e != cudaSuccess) return pz::set_error(PZ_EIO, "clearing the work counters: %s", cudaGetErrorString(e));
   }
   for (const auto& g : plan->groups) {  // phase 0 groups come before phase 1 of the same dtype
-    const int grid = std::min(plan->grid[g.dtype], g.total_tiles);
-    if (g.dtype == PZ_F32)
-      pz::launch_batch_f32(table + g.first_job, g.n_jobs, g.total_tiles, counters + g.counter, grid, s);
-    else
-      pz::launch_batch_f16(table + g.first_job, g.n_jobs, g.total_tiles, counters + g.counter, grid, s);
+    const int grid = std::min(plan->grid[g.dtype][g.hset], g.total_tiles);
+    auto* launch = g.dtype == PZ_F32 ? (g.hset ? pz::launch_batch_f32h : pz::launch_batch_f32)
+                                     : (g.hset ? pz::launch_batch_f16h : pz::launch_batch_f16);
+    launch(table + g.first_job, g.n_jobs, g.total_tiles, counters + g.counter, grid, s);
   }
   for (const pz_job& j : plan->nnedi3) {
     int rc = pz_run(j.model, j.in, j.n_planes, const_cast<pz_plane*>(j.out), j.n_planes, &j.opts, stream);

@@ -1,17 +1,6 @@
-// Persistent batch kernel, __half planes.
+// Persistent batch kernel, __half planes, FP32-texel programs and the ravu lattice.
 #include "batch_kernel.cuh"
 
 namespace pz {
-
-int launch_batch_f16(const DevJob* jobs, int n_jobs, int total, int* counter, int grid, cudaStream_t s) {
-  batch_kernel<__half><<<grid, kTileThreads, kBatchSmem, s>>>(jobs, n_jobs, total, counter);
-  return 0;
-}
-
-int batch_fit_f16() {
-  int fit = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, batch_kernel<__half>, kTileThreads, kBatchSmem);
-  return fit;
-}
-
+PZ_BATCH_DEFINE(f16, __half, false)
 }  // namespace pz

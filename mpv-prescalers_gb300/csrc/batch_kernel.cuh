@@ -13,7 +13,10 @@ enum Prog : int {
   kInt110 = 15,    // + (R-2)*3 + CM
   kLattice0 = 24,  // + (R-2)*3 + CM
   kZoom0 = 33,     // + (R-2)*6 + CM*2 + AR
-  kNumProgs = 45
+  kLiteH0 = 45,    // fast form (FP16 LUT texels): as kLite0
+  kThreeXH0 = 51,  //   as kThreeX0
+  kZoomH0 = 60,    //   as kZoom0
+  kNumProgs = 72
 };
 
 struct DevJob {
@@ -24,10 +27,15 @@ struct DevJob {
   int pad;
 };
 
-template <typename T>
+// H: the program set of the kernel -- false: programs 0..44 (FP32 LUT
+// texels, and the ravu lattice in every form); true: 45..71 (the fast form's
+// FP16-texel lite / 3x / zoom programs).  Two kernels per plane dtype keep
+// each translation unit's instantiations (and compile time) bounded.
+template <typename T, bool H>
 __device__ __forceinline__ void run_prog(int prog, const RavuArgs& a, int x0, int y0, float* smem) {
 #define PZ_CASE(id, ...) \
   case id: __VA_ARGS__::run(a, x0, y0, smem); return;
+  if constexpr (!H) {
   switch (prog) {
     PZ_CASE(0, LiteTile<2, false, T>) PZ_CASE(1, LiteTile<2, true, T>)
     PZ_CASE(2, LiteTile<3, false, T>) PZ_CASE(3, LiteTile<3, true, T>)
@@ -48,6 +56,24 @@ __device__ __forceinline__ void run_prog(int prog, const RavuArgs& a, int x0, in
     PZ_CASE(41, ZoomTile<3, kYuv, false, T>) PZ_CASE(42, ZoomTile<3, kYuv, true, T>)
     PZ_CASE(43, ZoomTile<3, kRgb, false, T>) PZ_CASE(44, ZoomTile<3, kRgb, true, T>)
   }
+  } else {
+  switch (prog) {
+    PZ_CASE(45, LiteTile<2, false, T, true>) PZ_CASE(46, LiteTile<2, true, T, true>)
+    PZ_CASE(47, LiteTile<3, false, T, true>) PZ_CASE(48, LiteTile<3, true, T, true>)
+    PZ_CASE(49, LiteTile<4, false, T, true>) PZ_CASE(50, LiteTile<4, true, T, true>)
+    PZ_CASE(51, ThreeXTile<2, kLuma, T, true>) PZ_CASE(52, ThreeXTile<2, kYuv, T, true>)
+    PZ_CASE(53, ThreeXTile<2, kRgb, T, true>) PZ_CASE(54, ThreeXTile<3, kLuma, T, true>)
+    PZ_CASE(55, ThreeXTile<3, kYuv, T, true>) PZ_CASE(56, ThreeXTile<3, kRgb, T, true>)
+    PZ_CASE(57, ThreeXTile<4, kLuma, T, true>) PZ_CASE(58, ThreeXTile<4, kYuv, T, true>)
+    PZ_CASE(59, ThreeXTile<4, kRgb, T, true>)
+    PZ_CASE(60, ZoomTile<2, kLuma, false, T, true>) PZ_CASE(61, ZoomTile<2, kLuma, true, T, true>)
+    PZ_CASE(62, ZoomTile<2, kYuv, false, T, true>) PZ_CASE(63, ZoomTile<2, kYuv, true, T, true>)
+    PZ_CASE(64, ZoomTile<2, kRgb, false, T, true>) PZ_CASE(65, ZoomTile<2, kRgb, true, T, true>)
+    PZ_CASE(66, ZoomTile<3, kLuma, false, T, true>) PZ_CASE(67, ZoomTile<3, kLuma, true, T, true>)
+    PZ_CASE(68, ZoomTile<3, kYuv, false, T, true>) PZ_CASE(69, ZoomTile<3, kYuv, true, T, true>)
+    PZ_CASE(70, ZoomTile<3, kRgb, false, T, true>) PZ_CASE(71, ZoomTile<3, kRgb, true, T, true>)
+  }
+  }
 #undef PZ_CASE
 }
 
@@ -57,7 +83,7 @@ constexpr size_t kBatchSmem = cmax(cmax(LatticeTile<4, kRgb, float>::smem_bytes,
                                    cmax(LiteTile<4, true, float>::smem_bytes, ThreeXTile<4, kRgb, float>::smem_bytes));
 
 // Persistent CTAs: claim tile numbers from `counter` until `total` is reached.
-template <typename T>
+template <typename T, bool H>
 __global__ void __launch_bounds__(kTileThreads) batch_kernel(const DevJob* __restrict__ jobs, int n_jobs, int total,
                                                              int* counter) {
   extern __shared__ float4 bsmem[];
@@ -90,15 +116,33 @@ __global__ void __launch_bounds__(kTileThreads) batch_kernel(const DevJob* __res
     }
     __syncthreads();
     const int t = item - s_first;
-    run_prog<T>(s_prog, s_args, (t % s_tw) * kTileW, (t / s_tw) * kTileH, smem);
+    run_prog<T, H>(s_prog, s_args, (t % s_tw) * kTileW, (t / s_tw) * kTileH, smem);
     __syncthreads();  // the tile's shared memory is free for the next claim
   }
 }
 
 
-int launch_batch_f32(const DevJob* jobs, int n_jobs, int total, int* counter, int grid, cudaStream_t s);
-int launch_batch_f16(const DevJob* jobs, int n_jobs, int total, int* counter, int grid, cudaStream_t s);
-int batch_fit_f32();
-int batch_fit_f16();
+// One persistent launch of the kernel for plane dtype `dt` (PZ_F32 / PZ_F16)
+// and program set `h`; batch_fit: its resident CTAs per SM.
+#define PZ_BATCH_DECL(sfx)                                                                          \
+  int launch_batch_##sfx(const DevJob* jobs, int n_jobs, int total, int* counter, int grid, cudaStream_t s); \
+  int batch_fit_##sfx();
+PZ_BATCH_DECL(f32)
+PZ_BATCH_DECL(f16)
+PZ_BATCH_DECL(f32h)
+PZ_BATCH_DECL(f16h)
+#undef PZ_BATCH_DECL
+
+// Instantiation of one (dtype, program set) kernel in its own translation unit.
+#define PZ_BATCH_DEFINE(sfx, T, H)                                                                  \
+  int launch_batch_##sfx(const DevJob* jobs, int n_jobs, int total, int* counter, int grid, cudaStream_t s) { \
+    batch_kernel<T, H><<<grid, kTileThreads, kBatchSmem, s>>>(jobs, n_jobs, total, counter);        \
+    return 0;                                                                                       \
+  }                                                                                                 \
+  int batch_fit_##sfx() {                                                                           \
+    int fit = 0;                                                                                    \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, batch_kernel<T, H>, kTileThreads, kBatchSmem); \
+    return fit;                                                                                     \
+  }
 
 }  // namespace pz

@@ -13,6 +13,7 @@ struct pz_model {
   float4* d_lut_ar = nullptr;
   float4* d_lut16 = nullptr;     // the LUTs with every value rounded to FP16
   float4* d_lut_ar16 = nullptr;
+  __half* d_lut_h = nullptr;     // the LUT as FP16 texels (fast form)
   int lut_rows = 0, lut_cols = 0;
   pz::KeyParams kp{};
   int nns = 0, win_w = 0, win_h = 0;
@@ -27,8 +28,19 @@ namespace pz {
 // Record `msg` for pz_last_error() on the calling thread; returns `code`.
 int set_error(int code, const char* fmt, ...);
 
+// Does the fast form read this model's LUT as FP16 texels?  The lite, 3x and
+// zoom programs gather a whole LUT row (or four bilinear texels per block)
+// per pixel and are bound by those L1 gathers; FP16 halves them.  The ravu
+// lattice reads 5-8 texels per key and keeps FP32, and so does ravu-zoom-ar's
+// anti-ringing LUT: most of its values lie below FP16's normal range.
+inline bool fast_half_lut(const pz_model* m, int precision) {
+  return precision == PZ_PREC_FAST &&
+         (m->family == PZ_RAVU_LITE || m->family == PZ_RAVU_3X || m->family == PZ_RAVU_ZOOM);
+}
+
 // The LUTs and LUT sampling of a precision form: the mpv form reads the
-// FP16-rounded copies and quantises zoom bilinear fractions to 1/256.
+// FP16-rounded copies and quantises zoom bilinear fractions to 1/256; the
+// fast form reads FP16 texels where fast_half_lut says so.
 inline void select_lut(const pz_model* m, int precision, RavuArgs* a) {
   const bool mpv = precision == PZ_PREC_MPV;
   a->lut = mpv ? m->d_lut16 : m->d_lut;
@@ -36,5 +48,7 @@ inline void select_lut(const pz_model* m, int precision, RavuArgs* a) {
   a->lut_rows = m->lut_rows;
   a->lut_cols = m->lut_cols;
   a->lut_frac = mpv ? 256.0f : 0.0f;
+  const bool h = fast_half_lut(m, precision);
+  a->lut_h = h ? reinterpret_cast<const uint2*>(m->d_lut_h) : nullptr;
 }
 }  // namespace pz

@@ -5,11 +5,12 @@
 namespace pz {
 namespace {
 
-template <typename T>
+template <typename T, bool H16>
 int launch_lite_t(const RavuArgs& a, int radius, bool ar, cudaStream_t s) {
   const int tw = (a.W + kTileW - 1) / kTileW, th = (a.H + kTileH - 1) / kTileH;
-#define PZ_LITE(R) \
-  return ar ? launch_tiles<LiteTile<R, true, T>>(a, tw, th, s) : launch_tiles<LiteTile<R, false, T>>(a, tw, th, s)
+#define PZ_LITE(R)                                                      \
+  return ar ? launch_tiles<LiteTile<R, true, T, H16>>(a, tw, th, s)     \
+            : launch_tiles<LiteTile<R, false, T, H16>>(a, tw, th, s)
   switch (radius) {
     case 2: PZ_LITE(2);
     case 3: PZ_LITE(3);
@@ -19,13 +20,13 @@ int launch_lite_t(const RavuArgs& a, int radius, bool ar, cudaStream_t s) {
   return -95;
 }
 
-template <typename T>
+template <typename T, bool H16>
 int launch_3x_t(const RavuArgs& a, int radius, int cm, cudaStream_t s) {
   const int tw = (a.W + kTileW - 1) / kTileW, th = (a.H + kTileH - 1) / kTileH;
 #define PZ_3X(R)                                                                         \
-  return cm == kLuma  ? launch_tiles<ThreeXTile<R, kLuma, T>>(a, tw, th, s)             \
-         : cm == kYuv ? launch_tiles<ThreeXTile<R, kYuv, T>>(a, tw, th, s)              \
-                      : launch_tiles<ThreeXTile<R, kRgb, T>>(a, tw, th, s)
+  return cm == kLuma  ? launch_tiles<ThreeXTile<R, kLuma, T, H16>>(a, tw, th, s)        \
+         : cm == kYuv ? launch_tiles<ThreeXTile<R, kYuv, T, H16>>(a, tw, th, s)         \
+                      : launch_tiles<ThreeXTile<R, kRgb, T, H16>>(a, tw, th, s)
   switch (radius) {
     case 2: PZ_3X(2);
     case 3: PZ_3X(3);
@@ -37,12 +38,17 @@ int launch_3x_t(const RavuArgs& a, int radius, int cm, cudaStream_t s) {
 
 }  // namespace
 
+// a.lut_h set (fast form): the programs read FP16 LUT texels
 int launch_lite(const RavuArgs& a, int radius, bool ar, int dtype, cudaStream_t s) {
-  return dtype == 0 ? launch_lite_t<float>(a, radius, ar, s) : launch_lite_t<__half>(a, radius, ar, s);
+  if (a.lut_h)
+    return dtype == 0 ? launch_lite_t<float, true>(a, radius, ar, s) : launch_lite_t<__half, true>(a, radius, ar, s);
+  return dtype == 0 ? launch_lite_t<float, false>(a, radius, ar, s) : launch_lite_t<__half, false>(a, radius, ar, s);
 }
 
 int launch_3x(const RavuArgs& a, int radius, int cm, int dtype, cudaStream_t s) {
-  return dtype == 0 ? launch_3x_t<float>(a, radius, cm, s) : launch_3x_t<__half>(a, radius, cm, s);
+  if (a.lut_h)
+    return dtype == 0 ? launch_3x_t<float, true>(a, radius, cm, s) : launch_3x_t<__half, true>(a, radius, cm, s);
+  return dtype == 0 ? launch_3x_t<float, false>(a, radius, cm, s) : launch_3x_t<__half, false>(a, radius, cm, s);
 }
 
 }  // namespace pz

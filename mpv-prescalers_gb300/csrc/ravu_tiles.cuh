@@ -127,6 +127,20 @@ __device__ __forceinline__ bool stage_frame(const RavuArgs& p, const TmaCtx* t, 
 }
 
 
+// One LUT texel: FP32 (float4) or, in the fast form, FP16 (4 halves in a
+// uint2, half the L1 traffic of the per-pixel row gathers).
+template <bool H16>
+__device__ __forceinline__ float4 lut_texel(const float4* f, const uint2* h, size_t i) {
+  if constexpr (H16) {
+    const uint2 q = __ldg(h + i);
+    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&q.x));
+    const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&q.y));
+    return make_float4(a.x, a.y, b.x, b.y);
+  } else {
+    return __ldg(f + i);
+  }
+}
+
 // ------------------------------------------------------------ ravu-lite ---
 // Does lite LUT column c take part in the anti-ringing sums?  r2: every
 // tap; r3/r4: the 13-tap diamond |dx|+|dy| <= 2 (ravu-lite-ar-r3.hook:93-170).
@@ -135,7 +149,7 @@ __host__ __device__ constexpr bool lite_ar_col(int c) {
   return R == 2 || cabs(c / (2 * R - 1) - (R - 1)) + cabs(c % (2 * R - 1) - (R - 1)) <= 2;
 }
 
-template <int R, bool AR, typename T>
+template <int R, bool AR, typename T, bool H16 = false>
 struct LiteTile {
   static constexpr int N = 2 * R - 1, S = N * N, HALO = R - 1;
   static constexpr int TW = kTileW + N - 1, TH = kTileH + N - 1;
@@ -157,7 +171,7 @@ struct LiteTile {
     structure_tensor<N, false>(get, p.kp, a, b, d);
     const int key = ravu_key(a, b, d, p.kp);
     if (p.keys) p.keys[(size_t)gy * p.W + gx] = key;
-    const float4* L = p.lut + (size_t)min(max(key, 0), p.lut_rows - 1) * p.lut_cols;
+    const size_t row = (size_t)min(max(key, 0), p.lut_rows - 1) * p.lut_cols;
     // FP32x2 sums: P = sum va*w, Q = sum vb*w, res = P + Q.wzyx; the
     // anti-ringing sums of output k as (hi, lo) and (hi2, lo2) pairs
     float2 P01 = make_float2(0.f, 0.f), P23 = P01, Q01 = P01, Q23 = P01;
@@ -166,7 +180,7 @@ struct LiteTile {
     for (int k = 0; k < 4; k++) HL[k] = HL3[k] = P01;
 #pragma unroll
     for (int c = 0; c < S / 2; c++) {
-      const float4 w = __ldg(L + c);
+      const float4 w = lut_texel<H16>(p.lut, p.lut_h, row + c);
       const float va = get(c / N, c % N), vb = get((S - 1 - c) / N, (S - 1 - c) % N);
       const float2 w01 = make_float2(w.x, w.y), w23 = make_float2(w.z, w.w);
       const float2 a2 = make_float2(va, va), b2 = make_float2(vb, vb);
@@ -191,7 +205,7 @@ struct LiteTile {
     }
     {
       constexpr int c = S / 2;
-      const float4 w = __ldg(L + c);
+      const float4 w = lut_texel<H16>(p.lut, p.lut_h, row + c);
       const float v = get(c / N, c % N);
       const float2 v2 = make_float2(v, v);
       P01 = __ffma2_rn(v2, make_float2(w.x, w.y), P01);
@@ -231,7 +245,7 @@ struct LiteTile {
 };
 
 // --------------------------------------------------------------- ravu-3x --
-template <int R, int CM, typename T>
+template <int R, int CM, typename T, bool H16 = false>
 struct ThreeXTile {
   static constexpr int N = 2 * R - 1, S = N * N, HALO = R - 1;
   static constexpr int TW = kTileW + N - 1, TH = kTileH + N - 1;
@@ -256,33 +270,51 @@ struct ThreeXTile {
     structure_tensor<N, false>(lum, p.kp, a, b, d);
     const int key = ravu_key(a, b, d, p.kp);
     if (p.keys) p.keys[(size_t)gy * p.W + gx] = key;
-    const float4* L = p.lut + (size_t)min(max(key, 0), p.lut_rows - 1) * p.lut_cols;
-    float4 r0[C], r1[C];
+    const size_t row = (size_t)min(max(key, 0), p.lut_rows - 1) * p.lut_cols;
+    // res0 += a*w0 + b*w1.wzyx; res1 += a*w1 + b*w0.wzyx, as FP32x2 sums
+    // P0 = sum a*w0, P1 = sum a*w1, Q0 = sum b*w0, Q1 = sum b*w1 (pairs .xy, .zw)
+    float2 P0[C][2], P1[C][2], Q0[C][2], Q1[C][2];
 #pragma unroll
-    for (int c = 0; c < C; c++) {
-      r0[c] = make_float4(0.f, 0.f, 0.f, 0.f);
-      r1[c] = r0[c];
-    }
+    for (int c = 0; c < C; c++)
+#pragma unroll
+      for (int h = 0; h < 2; h++) P0[c][h] = P1[c][h] = Q0[c][h] = Q1[c][h] = make_float2(0.f, 0.f);
 #pragma unroll
     for (int t = 0; t < S / 2; t++) {
-      const float4 w0 = __ldg(L + 2 * t), w1 = __ldg(L + 2 * t + 1);
+      const float4 w0 = lut_texel<H16>(p.lut, p.lut_h, row + 2 * t);
+      const float4 w1 = lut_texel<H16>(p.lut, p.lut_h, row + 2 * t + 1);
+      const float2 w0a = make_float2(w0.x, w0.y), w0b = make_float2(w0.z, w0.w);
+      const float2 w1a = make_float2(w1.x, w1.y), w1b = make_float2(w1.z, w1.w);
 #pragma unroll
       for (int c = 0; c < C; c++) {
         const float va = val(c, t), vb = val(c, S - 1 - t);
-        // res0 += a*w0 + b*w1.wzyx; res1 += a*w1 + b*w0.wzyx
-        r0[c].x += va * w0.x + vb * w1.w; r0[c].y += va * w0.y + vb * w1.z;
-        r0[c].z += va * w0.z + vb * w1.y; r0[c].w += va * w0.w + vb * w1.x;
-        r1[c].x += va * w1.x + vb * w0.w; r1[c].y += va * w1.y + vb * w0.z;
-        r1[c].z += va * w1.z + vb * w0.y; r1[c].w += va * w1.w + vb * w0.x;
+        const float2 a2 = make_float2(va, va), b2 = make_float2(vb, vb);
+        P0[c][0] = __ffma2_rn(a2, w0a, P0[c][0]);
+        P0[c][1] = __ffma2_rn(a2, w0b, P0[c][1]);
+        P1[c][0] = __ffma2_rn(a2, w1a, P1[c][0]);
+        P1[c][1] = __ffma2_rn(a2, w1b, P1[c][1]);
+        Q0[c][0] = __ffma2_rn(b2, w0a, Q0[c][0]);
+        Q0[c][1] = __ffma2_rn(b2, w0b, Q0[c][1]);
+        Q1[c][0] = __ffma2_rn(b2, w1a, Q1[c][0]);
+        Q1[c][1] = __ffma2_rn(b2, w1b, Q1[c][1]);
       }
     }
     constexpr int tc = S / 2;
-    const float4 w0 = __ldg(L + 2 * tc), w1 = __ldg(L + 2 * tc + 1);
+    const float4 w0 = lut_texel<H16>(p.lut, p.lut_h, row + 2 * tc);
+    const float4 w1 = lut_texel<H16>(p.lut, p.lut_h, row + 2 * tc + 1);
+    float4 r0[C], r1[C];
 #pragma unroll
     for (int c = 0; c < C; c++) {
       const float v = val(c, tc);
-      r0[c].x += v * w0.x; r0[c].y += v * w0.y; r0[c].z += v * w0.z; r0[c].w += v * w0.w;
-      r1[c].x += v * w1.x; r1[c].y += v * w1.y; r1[c].z += v * w1.z; r1[c].w += v * w1.w;
+      const float2 v2 = make_float2(v, v);
+      P0[c][0] = __ffma2_rn(v2, make_float2(w0.x, w0.y), P0[c][0]);
+      P0[c][1] = __ffma2_rn(v2, make_float2(w0.z, w0.w), P0[c][1]);
+      P1[c][0] = __ffma2_rn(v2, make_float2(w1.x, w1.y), P1[c][0]);
+      P1[c][1] = __ffma2_rn(v2, make_float2(w1.z, w1.w), P1[c][1]);
+      // r0 = P0 + Q1.wzyx, r1 = P1 + Q0.wzyx
+      r0[c] = make_float4(P0[c][0].x + Q1[c][1].y, P0[c][0].y + Q1[c][1].x, P0[c][1].x + Q1[c][0].y,
+                          P0[c][1].y + Q1[c][0].x);
+      r1[c] = make_float4(P1[c][0].x + Q0[c][1].y, P1[c][0].y + Q0[c][1].x, P1[c][1].x + Q0[c][0].y,
+                          P1[c][1].y + Q0[c][0].x);
       const float4 a0 = make_float4(clampf(r0[c].x, 0.f, 1.f), clampf(r0[c].y, 0.f, 1.f),
                                     clampf(r0[c].z, 0.f, 1.f), clampf(r0[c].w, 0.f, 1.f));
       const float4 a1 = make_float4(clampf(r1[c].x, 0.f, 1.f), clampf(r1[c].y, 0.f, 1.f),
@@ -476,8 +508,9 @@ __device__ __forceinline__ ZoomPos zoom_pos(int X, int W, int OW) {
 // (LUTPOS(x, 9) / (blocks, 288), ravu-zoom-r2.hook:23-31); clamp-to-edge.
 // With q > 0 the fractions are rounded to multiples of 1/q, as a texture
 // unit's fixed-point filter weights are (q = 256: 8 fractional bits).
-__device__ __forceinline__ float4 lut_bilinear(const float4* lut, int rows, int cols, int key, int blk, float sx,
-                                               float sy, float q) {
+template <bool H16>
+__device__ __forceinline__ float4 lut_bilinear(const float4* lut, const uint2* luth, int rows, int cols, int key,
+                                               int blk, float sx, float sy, float q) {
   const float fx8 = 8.0f * sx, fy8 = 8.0f * sy;
   const float x0f = floorf(fx8), y0f = floorf(fy8);
   float fx = fx8 - x0f, fy = fy8 - y0f;
@@ -487,8 +520,10 @@ __device__ __forceinline__ float4 lut_bilinear(const float4* lut, int rows, int 
   }
   const int xa = min(blk * 9 + (int)x0f, cols - 1), xb = min(xa + 1, cols - 1);
   const int ya = clampi(key * 9 + (int)y0f, 0, rows - 1), yb = min(ya + 1, rows - 1);
-  const float4 v00 = __ldg(lut + (size_t)ya * cols + xa), v01 = __ldg(lut + (size_t)ya * cols + xb);
-  const float4 v10 = __ldg(lut + (size_t)yb * cols + xa), v11 = __ldg(lut + (size_t)yb * cols + xb);
+  const float4 v00 = lut_texel<H16>(lut, luth, (size_t)ya * cols + xa);
+  const float4 v01 = lut_texel<H16>(lut, luth, (size_t)ya * cols + xb);
+  const float4 v10 = lut_texel<H16>(lut, luth, (size_t)yb * cols + xa);
+  const float4 v11 = lut_texel<H16>(lut, luth, (size_t)yb * cols + xb);
   const float gx = 1.0f - fx, gy = 1.0f - fy;
   float4 r;
   r.x = (v00.x * gx + v01.x * fx) * gy + (v10.x * gx + v11.x * fx) * fy;
@@ -504,7 +539,7 @@ __device__ __forceinline__ float comp4(const float4& v, int i) {
 
 // One thread per OUTPUT pixel; the tile is 32 x 8 output pixels and stages the
 // input rectangle they touch (at most (32+N+1) x (8+N+1) when upscaling).
-template <int R, int CM, bool AR, typename T>
+template <int R, int CM, bool AR, typename T, bool H16 = false>
 struct ZoomTile {
   static constexpr int N = 2 * R, S = N * N, LO = R - 1;
   static constexpr int RW = kTileW + N + 1, RH = kTileH + N + 1;
@@ -560,12 +595,13 @@ struct ZoomTile {
     }
 #pragma unroll
     for (int blk = 0; blk < NB; blk++) {
-      const float4 ws = lut_bilinear(p.lut, p.lut_rows, p.lut_cols, key, blk, sx, sy, p.lut_frac);
-      const float4 wi = lut_bilinear(p.lut, p.lut_rows, p.lut_cols, key, blk, ix, iy, p.lut_frac);
+      const float4 ws = lut_bilinear<H16>(p.lut, p.lut_h, p.lut_rows, p.lut_cols, key, blk, sx, sy, p.lut_frac);
+      const float4 wi = lut_bilinear<H16>(p.lut, p.lut_h, p.lut_rows, p.lut_cols, key, blk, ix, iy, p.lut_frac);
       float4 as = make_float4(0.f, 0.f, 0.f, 0.f), ai = as;
-      if (AR) {
-        as = lut_bilinear(p.lut_ar, p.lut_rows, p.lut_cols, key, blk, sx, sy, p.lut_frac);
-        ai = lut_bilinear(p.lut_ar, p.lut_rows, p.lut_cols, key, blk, ix, iy, p.lut_frac);
+      if (AR) {  // the anti-ringing LUT stays FP32 in every form but mpv's (most of
+                 // its values lie below FP16's normal range)
+        as = lut_bilinear<false>(p.lut_ar, nullptr, p.lut_rows, p.lut_cols, key, blk, sx, sy, p.lut_frac);
+        ai = lut_bilinear<false>(p.lut_ar, nullptr, p.lut_rows, p.lut_cols, key, blk, ix, iy, p.lut_frac);
       }
 #pragma unroll
       for (int j = 0; j < 4; j++) {

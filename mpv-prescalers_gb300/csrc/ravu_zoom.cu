@@ -5,12 +5,12 @@
 namespace pz {
 namespace {
 
-template <typename T>
+template <typename T, bool H16>
 int launch_t(const RavuArgs& a, int radius, int cm, bool ar, cudaStream_t s) {
   const int tw = (a.OW + kTileW - 1) / kTileW, th = (a.OH + kTileH - 1) / kTileH;
-#define PZ_Z(R, CM)                                                   \
-  return ar ? launch_tiles<ZoomTile<R, CM, true, T>>(a, tw, th, s)    \
-            : launch_tiles<ZoomTile<R, CM, false, T>>(a, tw, th, s)
+#define PZ_Z(R, CM)                                                        \
+  return ar ? launch_tiles<ZoomTile<R, CM, true, T, H16>>(a, tw, th, s)    \
+            : launch_tiles<ZoomTile<R, CM, false, T, H16>>(a, tw, th, s)
 #define PZ_Z_CM(R)                  \
   if (cm == kLuma) PZ_Z(R, kLuma);  \
   else if (cm == kYuv) PZ_Z(R, kYuv); \
@@ -27,7 +27,9 @@ int launch_t(const RavuArgs& a, int radius, int cm, bool ar, cudaStream_t s) {
 }  // namespace
 
 int launch_zoom(const RavuArgs& a, int radius, int cm, bool ar, int dtype, cudaStream_t s) {
-  return dtype == 0 ? launch_t<float>(a, radius, cm, ar, s) : launch_t<__half>(a, radius, cm, ar, s);
+  if (a.lut_h)  // fast form: FP16 LUT texels
+    return dtype == 0 ? launch_t<float, true>(a, radius, cm, ar, s) : launch_t<__half, true>(a, radius, cm, ar, s);
+  return dtype == 0 ? launch_t<float, false>(a, radius, cm, ar, s) : launch_t<__half, false>(a, radius, cm, ar, s);
 }
 
 }  // namespace pz

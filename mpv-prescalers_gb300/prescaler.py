@@ -251,7 +251,8 @@ class HookModel:
         ``out_size``: target ``(width, height)``; required for ravu-zoom,
         otherwise it only decides the ``//!WHEN`` conditions.
         ``precision``: "fp32" (plain FP32 arithmetic), "fast" (FP16
-        tensor-core NNEDI3 neurons; RAVU arithmetic stays FP32) or "mpv"
+        tensor-core NNEDI3 neurons; ravu-lite / 3x / zoom LUTs read as FP16
+        texels, all RAVU arithmetic FP32) or "mpv"
         (what the mpv host computes, to measure the distance to it: FP16
         planes only, LUTs rounded to FP16, ravu-zoom LUT bilinear weights
         in 1/256 steps; NNEDI3 as "fp32").

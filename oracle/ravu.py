@@ -450,15 +450,16 @@ def ravu_zoom(model, planes, out_w: int, out_h: int, keys: Optional[np.ndarray] 
     return res, info
 
 
-def mpv_form(model):
+def mpv_form(model, round_ar: bool = True):
     """The model as the mpv host holds it: every LUT value rounded to FP16
     (the //!TEXTURE blocks are uploaded as ``//!FORMAT rgba16f``,
     ``ravu-lite-r3.hook:134``).  Use with ``frac_steps=256`` for ravu-zoom
-    and FP16 planes to restate what the host computes."""
+    and FP16 planes to restate what the host computes.  ``round_ar=False``
+    leaves ravu-zoom-ar's anti-ringing LUT exact (the library's fast form)."""
     import copy
     m = copy.copy(model)
     m.lut = np.asarray(model.lut, dtype=np.float32).astype(np.float16).astype(np.float32)
-    if getattr(model, "lut_ar", None) is not None:
+    if round_ar and getattr(model, "lut_ar", None) is not None:
         m.lut_ar = np.asarray(model.lut_ar, dtype=np.float32).astype(np.float16).astype(np.float32)
     return m
 

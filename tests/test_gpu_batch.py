@@ -30,6 +30,11 @@ MIX = [  # (model, H, W, dtype, out_size, precision)
     ("ravu-3x-r3-rgb", 11, 13, torch.float32, None, "fp32"),
     ("nnedi3-nns32-win8x4", 40, 48, torch.float32, None, "fast"),
     ("nnedi3-nns16-win8x6", 24, 30, torch.float16, None, "fp32"),
+    # the fast form's FP16-texel programs run in their own persistent launch
+    ("ravu-lite-ar-r4", 33, 70, torch.float16, None, "fast"),
+    ("ravu-3x-r3-yuv", 14, 19, torch.float16, None, "fast"),
+    ("ravu-zoom-ar-r2", 22, 35, torch.float32, (60, 41), "fast"),
+    ("ravu-r3", 20, 26, torch.float16, None, "fast"),
 ]
 
 

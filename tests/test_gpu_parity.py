@@ -44,7 +44,7 @@ def _run_gpu(hm, x, out_size, dtype=torch.float32, precision="fp32"):
     return y.float().cpu().numpy().astype(np.float64), keys.cpu().numpy()
 
 
-def _check_keyed(hm, x, out_size, tol=TOL_FP32, dtype=torch.float32):
+def _check_keyed(hm, x, out_size, tol=TOL_FP32, dtype=torch.float32, precision="fp32", oracle_model=None):
     """Keys and values of the GPU against the oracle.
 
     For the ravu lattice the int10/int01 passes read int11; they are checked
@@ -53,8 +53,8 @@ def _check_keyed(hm, x, out_size, tol=TOL_FP32, dtype=torch.float32):
     Returns (key mismatches, boundary keys, max-abs with identical keys,
     PSNR against the unforced oracle).
     """
-    m = hm.model
-    y, kg = _run_gpu(hm, x, out_size, dtype=dtype)
+    m = hm.model if oracle_model is None else oracle_model
+    y, kg = _run_gpu(hm, x, out_size, dtype=dtype, precision=precision)
     over = y[:, 1::2, 1::2] if m.family == "ravu" else None
     ref, info = oracle.keyed_upscale(m, x, out_size, int11=over)
     forced, _ = oracle.keyed_upscale(m, x, out_size, keys=kg, int11=over)
@@ -154,6 +154,39 @@ def test_fp16_planes_meet_quality_bar(name):
     x16 = x.astype(np.float16).astype(np.float32)
     out_size = {"zoom": (150, 100), "3x": (3 * W, 3 * H)}.get(hm.family, (2 * W, 2 * H))
     _mism, _bnd, err, psnr = _check_keyed(hm, x16, out_size, tol=TOL_FP16_MAXABS, dtype=torch.float16)
+    assert psnr >= TOL_FP16_PSNR, f"{name}: PSNR {psnr:.1f} dB"
+
+
+FAST_RAVU = ["ravu-lite-r2", "ravu-lite-ar-r3", "ravu-lite-ar-r4", "ravu-3x-r2", "ravu-3x-r4-yuv", "ravu-3x-r3-rgb",
+             "ravu-zoom-r3", "ravu-zoom-ar-r2", "ravu-zoom-ar-r2-rgb", "ravu-r3"]
+
+
+@pytest.mark.parametrize("name", FAST_RAVU)
+def test_ravu_fast_form_is_fp32_math_on_fp16_lut_texels(name):
+    """precision="fast" reads the lite / 3x / zoom LUTs as FP16 texels and
+    keeps every operation FP32: on FP32 planes it matches the oracle run
+    with those LUTs rounded to FP16 to the plain-FP32 bar (keys, 1e-5)."""
+    hm = _model(name)
+    H, W = 37, 45
+    x = synth.frame(H, W, 67, hm.channels)
+    out_size = {"zoom": (100, 71), "3x": (3 * W, 3 * H)}.get(hm.family, (2 * W, 2 * H))
+    # the ravu lattice and zoom-ar's anti-ringing LUT keep FP32 texels
+    m16 = oracle.mpv_form(hm.model, round_ar=False) if hm.family != "ravu" else hm.model
+    _check_keyed(hm, x, out_size, precision="fast", oracle_model=m16)
+
+
+@pytest.mark.parametrize("name", ["ravu-lite-ar-r3", "ravu-lite-ar-r4", "ravu-lite-r3", "ravu-3x-r3",
+                                  "ravu-zoom-ar-r2-rgb", "ravu-zoom-r3-yuv"])
+def test_ravu_fast_form_meets_quality_bar(name):
+    """The chosen form (FP16 planes, FP16 LUT texels, FP32 math) against the
+    exact-LUT FP64 oracle: max-abs <= 2e-3 with the GPU's keys, PSNR >= 55 dB
+    unforced."""
+    hm = _model(name)
+    H, W = 64, 96
+    x = synth.frame(H, W, 63, hm.channels).astype(np.float16).astype(np.float32)
+    out_size = {"zoom": (150, 100), "3x": (3 * W, 3 * H)}.get(hm.family, (2 * W, 2 * H))
+    _mism, _bnd, err, psnr = _check_keyed(hm, x, out_size, tol=TOL_FP16_MAXABS, dtype=torch.float16,
+                                          precision="fast")
     assert psnr >= TOL_FP16_PSNR, f"{name}: PSNR {psnr:.1f} dB"
 
 
