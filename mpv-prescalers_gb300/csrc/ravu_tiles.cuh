@@ -333,6 +333,41 @@ struct ThreeXTile {
   }
 };
 
+// The ravu keyed filter of one key evaluation: res[c] = sum over the S/2
+// mirrored tap pairs of (x_i + x_{S-1-i}) * w_i (ravu-r3.hook:126-146), the
+// weights w_i packed 4 to a texel.  Two tap pairs per FP32x2 FADD/FFMA.
+template <int S, int C, class Val>
+__device__ __forceinline__ void ravu_filter(const float4* L, const Val& val, float (&res)[C]) {
+  float2 acc[C];
+#pragma unroll
+  for (int c = 0; c < C; c++) acc[c] = make_float2(0.0f, 0.0f);
+#pragma unroll
+  for (int q = 0; q < (S / 2 + 3) / 4; q++) {
+    const float4 w4 = __ldg(L + q);
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int i0 = 4 * q + 2 * h, i1 = i0 + 1;
+      const float2 w2 = h == 0 ? make_float2(w4.x, w4.y) : make_float2(w4.z, w4.w);
+      if (i1 < S / 2) {
+#pragma unroll
+        for (int c = 0; c < C; c++) {
+          const float2 s2 = __fadd2_rn(make_float2(val(c, i0), val(c, i1)),
+                                       make_float2(val(c, S - 1 - i0), val(c, S - 1 - i1)));
+          acc[c] = __ffma2_rn(s2, w2, acc[c]);
+        }
+      } else if (i0 < S / 2) {
+#pragma unroll
+        for (int c = 0; c < C; c++) acc[c].x = fmaf(val(c, i0) + val(c, S - 1 - i0), w2.x, acc[c].x);
+      }
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < C; c++) res[c] = acc[c].x + acc[c].y;
+}
+
+// ------------------------------------------------------ ravu lattice -----
+// int11: the keyed filter over the input window.  Writes int11 and the input
+// copy straight into the output plane at (2i+1, 2j+1) and (2i, 2j).
 // ------------------------------------------------------ ravu lattice -----
 // int11: the keyed filter over the input window.  Writes int11 and the input
 // copy straight into the output plane at (2i+1, 2j+1) and (2i, 2j).
@@ -363,21 +398,7 @@ struct Int11Tile {
     if (p.keys) p.keys[(size_t)gy * p.W + gx] = key;
     const float4* L = p.lut + (size_t)min(max(key, 0), p.lut_rows - 1) * p.lut_cols;
     float res[C];
-#pragma unroll
-    for (int c = 0; c < C; c++) res[c] = 0.0f;
-#pragma unroll
-    for (int q = 0; q < (S / 2 + 3) / 4; q++) {
-      const float4 w4 = __ldg(L + q);
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        const int i = 4 * q + j;
-        if (i < S / 2) {
-          const float w = j == 0 ? w4.x : (j == 1 ? w4.y : (j == 2 ? w4.z : w4.w));
-#pragma unroll
-          for (int c = 0; c < C; c++) res[c] += (val(c, i) + val(c, S - 1 - i)) * w;
-        }
-      }
-    }
+    ravu_filter<S, C>(L, val, res);
 #pragma unroll
     for (int c = 0; c < C; c++) {
       T* o = static_cast<T*>(p.out[c]);
@@ -461,21 +482,7 @@ struct LatticeTile {
       if (p.keys) p.keys[(size_t)(1 + L) * p.W * p.H + (size_t)gy * p.W + gx] = key;
       const float4* Lr = p.lut + (size_t)min(max(key, 0), p.lut_rows - 1) * p.lut_cols;
       float res[C];
-#pragma unroll
-      for (int c = 0; c < C; c++) res[c] = 0.0f;
-#pragma unroll
-      for (int q = 0; q < (S / 2 + 3) / 4; q++) {
-        const float4 w4 = __ldg(Lr + q);
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-          const int i = 4 * q + j;
-          if (i < S / 2) {
-            const float w = j == 0 ? w4.x : (j == 1 ? w4.y : (j == 2 ? w4.z : w4.w));
-#pragma unroll
-            for (int c = 0; c < C; c++) res[c] += (val(c, i) + val(c, S - 1 - i)) * w;
-          }
-        }
-      }
+      ravu_filter<S, C>(Lr, val, res);
 #pragma unroll
       for (int c = 0; c < C; c++) {
         T* o = static_cast<T*>(p.out[c]);
