@@ -361,7 +361,11 @@ def run_gpu(args):
                      "hbm": {"achieved": algo_bytes / (kern_ms / 1e3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
                              "frac": algo_bytes / (kern_ms / 1e3) / 1e9 / hbm_peak,
                              "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
-                     "traffic": None},
+                     # dram__bytes_read.sum + dram__bytes_write.sum of this kernel on one 1080p
+                     # frame (ncu, profiles/lite_tile_h16_ravu-lite-ar-r4_1080p_fp16.md): the FP16
+                     # input plane; the 16.6 MB output is still in L2 when the launch ends
+                     "traffic": 4221440, "traffic_unit": "bytes per launch",
+                     "algorithmic_bytes": algo_bytes},
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clocks,
         "headline": headline,

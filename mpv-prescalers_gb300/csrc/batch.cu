@@ -1,12 +1,16 @@
-// Batched execution: many frames (any sizes) of many RAVU models in one
-// persistent launch, plus the NNEDI3 jobs of the batch.
+// Batched execution: many frames (any sizes) of many RAVU models in a few
+// persistent launches, plus the NNEDI3 jobs of the batch.
 //
 // The reference runs one shader dispatch per pass per frame; a player with
 // several streams issues them back to back.  Here a plan uploads one table of
-// job descriptors to caller-provided device memory; each launch then
-//   phase 0: one persistent kernel per plane dtype runs every first-pass tile
-//            of every job (ravu-lite, ravu-3x, ravu-zoom, ravu int11), CTAs
-//            pulling tile numbers from a device counter;
+// job descriptors to caller-provided device memory, grouped by tile program
+// (family, radius, channels, anti-ringing, LUT form) and plane dtype; each
+// launch then runs
+//   phase 0: per group, one persistent kernel of that program over every
+//            first-pass tile of the group's frames (ravu-lite, ravu-3x,
+//            ravu-zoom, ravu int11), CTAs pulling tile numbers from the
+//            group's device counter -- register use and shared memory are the
+//            program's own, as in a per-frame launch;
 //   phase 1: the same for the ravu lattice pass (int10/int01), which reads
 //            the int11 values phase 0 wrote;
 //   NNEDI3 jobs are stream-ordered launches of their two passes.
@@ -19,7 +23,7 @@
 
 #include "../../include/prescale.h"
 #include "model.h"
-#include "batch_kernel.cuh"
+#include "ravu_tiles.cuh"
 
 namespace pz {
 namespace {
@@ -45,74 +49,102 @@ int* device_error_word();
 
 // Host plan: what one launch enqueues.
 struct pz_batch {
-  struct Group {  // one persistent launch
-    int dtype;
+  struct Group {  // one persistent launch: one program, one plane dtype
     int phase;
-    int hset;       // program set: 1 = the fast form's FP16-texel programs
-    int first_job;  // index into the device table
+    int dtype;
+    int prog;
+    int first_job;    // index into the device table
     int n_jobs;
     int total_tiles;
-    int counter;    // index of its counter int
+    int grid;
+    pz::PersistentOps ops;
   };
-  std::vector<Group> groups;
+  std::vector<Group> groups;   // phase 0 groups, then phase 1
   std::vector<pz_job> nnedi3;  // run as their own launches
   void* work = nullptr;
-  int n_counters = 0;
-  int ctas_per_sm = 0;         // 0 = as many as fit
-  int grid[2][2] = {{0, 0}, {0, 0}};  // per dtype and program set
+  size_t table_offset = 0;     // the counters (one int per group) come first
 };
 
 namespace {
 
-int build_tables(const pz_job* jobs, int n, std::vector<pz::DevJob>* table, pz_batch* plan, int phase_filter) {
-  (void)phase_filter;
-  for (int dt = 0; dt < 2; dt++) {
-    for (int phase = 0; phase < 2; phase++) {
-     for (int hset = 0; hset < 2; hset++) {
-      pz_batch::Group g{dt, phase, hset, (int)table->size(), 0, 0, plan->n_counters};
-      for (int i = 0; i < n; i++) {
-        const pz_job& j = jobs[i];
-        const pz_model* m = j.model;
-        if (m->family == PZ_NNEDI3) continue;
-        if (j.in[0].dtype != dt) continue;
-        if (phase == 1 && m->family != PZ_RAVU) continue;
-        if (pz::fast_half_lut(m, j.opts.precision) != (hset == 1)) continue;
-        pz::DevJob d{};
-        pz::RavuArgs& a = d.a;
-        const int C = m->channels == PZ_LUMA ? 1 : 3;
-        for (int c = 0; c < C; c++) {
-          a.in[c] = j.in[c].data;
-          a.in_pitch[c] = j.in[c].pitch;
-          a.out[c] = j.out[c].data;
-          a.out_pitch[c] = j.out[c].pitch;
-        }
-        a.W = j.in[0].width;
-        a.H = j.in[0].height;
-        a.OW = j.out[0].width;
-        a.OH = j.out[0].height;
-        pz::select_lut(m, j.opts.precision, &a);
-        a.ar = m->ar;
-        a.keys = nullptr;
-        a.err = pz::device_error_word();
-        a.kp = m->kp;
-        d.prog = pz::prog_of(m, j.opts.precision) + (phase == 1 ? pz::kLattice0 - pz::kInt110 : 0);
-        const bool zoom = m->family == PZ_RAVU_ZOOM;
-        const int tw = ((zoom ? a.OW : a.W) + pz::kTileW - 1) / pz::kTileW;
-        const int th = ((zoom ? a.OH : a.H) + pz::kTileH - 1) / pz::kTileH;
-        d.tiles_w = tw;
-        d.first_tile = g.total_tiles;
-        g.total_tiles += tw * th;
-        table->push_back(d);
-        g.n_jobs++;
-      }
-      if (g.n_jobs) {
-        plan->groups.push_back(g);
-        plan->n_counters++;
-      }
-     }
+pz::PersistentOps ops_of(int prog, int dtype) {
+  if (prog >= pz::kInt110 && prog < pz::kZoom0) return pz::persistent_ops_lattice(prog, dtype);
+  if ((prog >= pz::kZoom0 && prog < pz::kLiteH0) || prog >= pz::kZoomH0) return pz::persistent_ops_zoom(prog, dtype);
+  return pz::persistent_ops_lite(prog, dtype);
+}
+
+// Table entries of the RAVU jobs (one per job and phase), grouped by
+// (phase, dtype, program) with each group's tile prefix sums.
+int build_tables(const pz_job* jobs, int n, std::vector<pz::DevJob>* table, pz_batch* plan) {
+  struct Entry {
+    int phase, dtype, prog, job;
+  };
+  std::vector<Entry> entries;
+  for (int i = 0; i < n; i++) {
+    const pz_model* m = jobs[i].model;
+    if (m->family == PZ_NNEDI3) continue;
+    const int prog = pz::prog_of(m, jobs[i].opts.precision);
+    entries.push_back({0, jobs[i].in[0].dtype, prog, i});
+    if (m->family == PZ_RAVU) entries.push_back({1, jobs[i].in[0].dtype, prog + pz::kLattice0 - pz::kInt110, i});
+  }
+  std::stable_sort(entries.begin(), entries.end(), [](const Entry& a, const Entry& b) {
+    if (a.phase != b.phase) return a.phase < b.phase;
+    if (a.dtype != b.dtype) return a.dtype < b.dtype;
+    return a.prog < b.prog;
+  });
+  for (size_t e = 0; e < entries.size(); e++) {
+    const Entry& en = entries[e];
+    if (plan->groups.empty() || plan->groups.back().phase != en.phase || plan->groups.back().dtype != en.dtype ||
+        plan->groups.back().prog != en.prog) {
+      pz_batch::Group g{};
+      g.phase = en.phase;
+      g.dtype = en.dtype;
+      g.prog = en.prog;
+      g.first_job = (int)table->size();
+      g.ops = ops_of(en.prog, en.dtype);
+      if (!g.ops.launch) return pz::set_error(PZ_ENOTSUP, "no persistent kernel for program %d", en.prog);
+      plan->groups.push_back(g);
     }
+    pz_batch::Group& g = plan->groups.back();
+    const pz_job& j = jobs[en.job];
+    const pz_model* m = j.model;
+    pz::DevJob d{};
+    pz::RavuArgs& a = d.a;
+    const int C = m->channels == PZ_LUMA ? 1 : 3;
+    for (int c = 0; c < C; c++) {
+      a.in[c] = j.in[c].data;
+      a.in_pitch[c] = j.in[c].pitch;
+      a.out[c] = j.out[c].data;
+      a.out_pitch[c] = j.out[c].pitch;
+    }
+    a.W = j.in[0].width;
+    a.H = j.in[0].height;
+    a.OW = j.out[0].width;
+    a.OH = j.out[0].height;
+    pz::select_lut(m, j.opts.precision, &a);
+    a.ar = m->ar;
+    a.keys = nullptr;
+    a.err = pz::device_error_word();
+    a.kp = m->kp;
+    d.prog = en.prog;
+    const bool zoom = m->family == PZ_RAVU_ZOOM;
+    const int tw = ((zoom ? a.OW : a.W) + pz::kTileW - 1) / pz::kTileW;
+    const int th = ((zoom ? a.OH : a.H) + pz::kTileH - 1) / pz::kTileH;
+    d.tiles_w = tw;
+    d.first_tile = g.total_tiles;
+    g.total_tiles += tw * th;
+    table->push_back(d);
+    g.n_jobs++;
   }
   return PZ_OK;
+}
+
+// Table entries (= the most groups) of a job list.
+size_t n_entries(const pz_job* jobs, int n_jobs) {
+  size_t n = 0;
+  for (int i = 0; i < n_jobs; i++)
+    if (jobs[i].model && jobs[i].model->family != PZ_NNEDI3) n += jobs[i].model->family == PZ_RAVU ? 2 : 1;
+  return n;
 }
 
 int validate_job(const pz_job& j, int idx) {
@@ -164,10 +196,8 @@ extern "C" {
 
 size_t pz_batch_work_bytes(const pz_job* jobs, int n_jobs) {
   if (!jobs || n_jobs <= 0) return 0;
-  size_t n = 0;
-  for (int i = 0; i < n_jobs; i++)
-    if (jobs[i].model && jobs[i].model->family != PZ_NNEDI3) n += jobs[i].model->family == PZ_RAVU ? 2 : 1;
-  return pz::align256(8 * sizeof(int)) + n * sizeof(pz::DevJob);
+  const size_t n = n_entries(jobs, n_jobs);
+  return pz::align256(n * sizeof(int)) + n * sizeof(pz::DevJob);
 }
 
 int pz_batch_create(const pz_job* jobs, int n_jobs, void* work, size_t work_bytes, int ctas_per_sm, void* stream,
@@ -183,14 +213,17 @@ int pz_batch_create(const pz_job* jobs, int n_jobs, void* work, size_t work_byte
   pz_batch* plan = new (std::nothrow) pz_batch();
   if (!plan) return pz::set_error(PZ_ENOMEM, "host allocation failed");
   std::vector<pz::DevJob> table;
-  build_tables(jobs, n_jobs, &table, plan, 0);
+  if ((rc = build_tables(jobs, n_jobs, &table, plan))) {
+    delete plan;
+    return rc;
+  }
   for (int i = 0; i < n_jobs; i++)
     if (jobs[i].model->family == PZ_NNEDI3) plan->nnedi3.push_back(jobs[i]);
   plan->work = work;
-  plan->ctas_per_sm = ctas_per_sm;
+  plan->table_offset = pz::align256(n_entries(jobs, n_jobs) * sizeof(int));
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (!table.empty()) {
-    cudaError_t e = cudaMemcpyAsync(static_cast<char*>(work) + pz::align256(8 * sizeof(int)), table.data(),
+    cudaError_t e = cudaMemcpyAsync(static_cast<char*>(work) + plan->table_offset, table.data(),
                                     table.size() * sizeof(pz::DevJob), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // the table is pageable host memory
     if (e != cudaSuccess) {
@@ -201,14 +234,11 @@ int pz_batch_create(const pz_job* jobs, int n_jobs, void* work, size_t work_byte
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  for (int dt = 0; dt < 2; dt++) {
-    for (int h = 0; h < 2; h++) {
-      int fit = dt == 0 ? (h ? pz::batch_fit_f32h() : pz::batch_fit_f32())
-                        : (h ? pz::batch_fit_f16h() : pz::batch_fit_f16());
-      if (fit < 1) fit = 1;
-      const int per = ctas_per_sm > 0 ? std::min(ctas_per_sm, fit) : fit;
-      plan->grid[dt][h] = per * sms;
-    }
+  for (auto& g : plan->groups) {
+    int fit = g.ops.fit();
+    if (fit < 1) fit = 1;
+    const int per = ctas_per_sm > 0 ? std::min(ctas_per_sm, fit) : fit;
+    g.grid = std::min(per * sms, g.total_tiles);
   }
   *out = plan;
   return PZ_OK;
@@ -218,17 +248,14 @@ int pz_batch_launch(const pz_batch* plan, void* stream) {
   if (!plan) return pz::set_error(PZ_EINVAL, "null plan");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int* counters = static_cast<int*>(plan->work);
-  const pz::DevJob* table =
-      reinterpret_cast<const pz::DevJob*>(static_cast<char*>(plan->work) + pz::align256(8 * sizeof(int)));
+  const pz::DevJob* table = reinterpret_cast<const pz::DevJob*>(static_cast<char*>(plan->work) + plan->table_offset);
   if (!plan->groups.empty()) {
-    cudaError_t e = cudaMemsetAsync(counters, 0, 8 * sizeof(int), s);
+    cudaError_t e = cudaMemsetAsync(counters, 0, plan->groups.size() * sizeof(int), s);
     if (e != cudaSuccess) return pz::set_error(PZ_EIO, "clearing the work counters: %s", cudaGetErrorString(e));
   }
-  for (const auto& g : plan->groups) {  // phase 0 groups come before phase 1 of the same dtype
-    const int grid = std::min(plan->grid[g.dtype][g.hset], g.total_tiles);
-    auto* launch = g.dtype == PZ_F32 ? (g.hset ? pz::launch_batch_f32h : pz::launch_batch_f32)
-                                     : (g.hset ? pz::launch_batch_f16h : pz::launch_batch_f16);
-    launch(table + g.first_job, g.n_jobs, g.total_tiles, counters + g.counter, grid, s);
+  for (size_t i = 0; i < plan->groups.size(); i++) {  // phase 0 groups come before phase 1
+    const auto& g = plan->groups[i];
+    g.ops.launch(table + g.first_job, g.n_jobs, g.total_tiles, counters + i, g.grid, s);
   }
   for (const pz_job& j : plan->nnedi3) {
     int rc = pz_run(j.model, j.in, j.n_planes, const_cast<pz_plane*>(j.out), j.n_planes, &j.opts, stream);

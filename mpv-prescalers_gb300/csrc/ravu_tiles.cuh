@@ -690,4 +690,98 @@ int launch_tiles(const RavuArgs& a, int tiles_w, int tiles_h, cudaStream_t s) {
   return 0;
 }
 
+// ------------------------------------------------------ persistent batches ---
+// Program ids of a batch job (tile program and form; see batch.cu).
+enum ProgId : int {
+  kLite0 = 0,      // + (R-2)*2 + AR
+  kThreeX0 = 6,    // + (R-2)*3 + CM
+  kInt110 = 15,    // + (R-2)*3 + CM
+  kLattice0 = 24,  // + (R-2)*3 + CM
+  kZoom0 = 33,     // + (R-2)*6 + CM*2 + AR
+  kLiteH0 = 45,    // fast form (FP16 LUT texels): as kLite0
+  kThreeXH0 = 51,  //   as kThreeX0
+  kZoomH0 = 60,    //   as kZoom0
+  kNumProgs = 72
+};
+
+// One batch job: a frame's arguments and its place in its launch's tile range.
+struct DevJob {
+  RavuArgs a;
+  int prog;
+  int tiles_w;
+  int first_tile;  // prefix sum within its launch group
+  int pad;
+};
+
+// Persistent CTAs of one tile program: claim tile numbers from `counter`
+// until `total`; a tile's job is the last whose first tile <= the number
+// (binary search over the group's prefix sums); the job's arguments are
+// copied to shared memory when the job changes.  Every job of a launch runs
+// the same program, so register use and shared memory are the program's own.
+template <class Prog>
+__global__ void __launch_bounds__(kTileThreads) persistent_kernel(const DevJob* __restrict__ jobs, int n_jobs,
+                                                                  int total, int* counter) {
+  extern __shared__ __align__(128) float4 psmem[];
+  float* smem = reinterpret_cast<float*>(psmem);
+  __shared__ RavuArgs s_args;
+  __shared__ int s_item, s_job, s_tw, s_first;
+  int loaded = -1;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const int item = atomicAdd(counter, 1);
+      s_item = item;
+      if (item < total) {
+        int lo = 0, hi = n_jobs - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (jobs[mid].first_tile <= item) lo = mid; else hi = mid - 1;
+        }
+        s_job = lo;
+        s_tw = jobs[lo].tiles_w;
+        s_first = jobs[lo].first_tile;
+      }
+    }
+    __syncthreads();
+    const int item = s_item;
+    if (item >= total) break;
+    if (s_job != loaded) {  // uniform: every thread reads the same s_job
+      loaded = s_job;
+      const int* src = reinterpret_cast<const int*>(&jobs[loaded].a);
+      int* dst = reinterpret_cast<int*>(&s_args);
+      for (int i = threadIdx.x; i < (int)(sizeof(RavuArgs) / 4); i += kTileThreads) dst[i] = src[i];
+      __syncthreads();
+    }
+    const int t = item - s_first;
+    Prog::run(s_args, (t % s_tw) * kTileW, (t / s_tw) * kTileH, smem, nullptr);
+    __syncthreads();  // the tile's shared memory and s_item are free for the next claim
+  }
+}
+
+// Launch and occupancy query of one program's persistent kernel.
+struct PersistentOps {
+  void (*launch)(const DevJob* jobs, int n_jobs, int total, int* counter, int grid, cudaStream_t s);
+  int (*fit)();  // resident CTAs per SM
+};
+
+template <class Prog>
+PersistentOps persistent_ops() {
+  static_assert(Prog::smem_bytes <= 48 * 1024, "tile program needs more than the default shared memory");
+  return {[](const DevJob* j, int n, int total, int* c, int grid, cudaStream_t s) {
+            persistent_kernel<Prog><<<grid, kTileThreads, Prog::smem_bytes, s>>>(j, n, total, c);
+          },
+          []() {
+            int fit = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, persistent_kernel<Prog>, kTileThreads,
+                                                          Prog::smem_bytes);
+            return fit;
+          }};
+}
+
+// The ops of program `prog` for plane dtype `dtype` (0 FP32, 1 FP16), or
+// null members when `prog` is not the family's; defined beside the family's
+// per-frame launchers.
+PersistentOps persistent_ops_lite(int prog, int dtype);     // lite, 3x (ravu_lite.cu)
+PersistentOps persistent_ops_lattice(int prog, int dtype);  // int11, lattice (ravu_lattice.cu)
+PersistentOps persistent_ops_zoom(int prog, int dtype);     // zoom (ravu_zoom.cu)
+
 }  // namespace pz
