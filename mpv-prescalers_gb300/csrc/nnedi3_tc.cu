@@ -167,12 +167,30 @@ __global__ void __launch_bounds__(kThreads) nn_tc_kernel(const __grid_constant__
   const int ntiles = tiles_x * tiles_y;
   uint32_t phase = 0;  // bit b: parity of mbar[b]'s next phase
 
+  // the window tile of the next tile is loaded into registers while the
+  // current tile's neurons run (at most PF values per thread)
+  constexpr int PF = (TW * TH + kThreads - 1) / kThreads;
+  float pre[PF];
+  auto prefetch = [&](int tid_) {
+    if (tid_ >= ntiles) return;
+    const int px0 = (tid_ % tiles_x) * 32, py0 = (tid_ / tiles_x) * 4;
+#pragma unroll
+    for (int r = 0; r < PF; r++) {
+      const int i = tid + r * kThreads;
+      if (i < TW * TH) {
+        const int ty = i / TW, tx = i % TW;
+        const int gx = clampi(px0 + OX0 + tx, 0, p.W - 1), gy = clampi(py0 + OY0 + ty, 0, p.H - 1);
+        pre[r] = ldp(in + (size_t)gy * p.in_pitch + gx);
+      }
+    }
+  };
+  prefetch(blockIdx.x);
   for (int tile_id = blockIdx.x; tile_id < ntiles; tile_id += gridDim.x) {
     const int x0 = (tile_id % tiles_x) * 32, y0 = (tile_id / tiles_x) * 4;
-    for (int i = tid; i < TW * TH; i += kThreads) {
-      int ty = i / TW, tx = i % TW;
-      int gx = clampi(x0 + OX0 + tx, 0, p.W - 1), gy = clampi(y0 + OY0 + ty, 0, p.H - 1);
-      tile[i] = ldp(in + (size_t)gy * p.in_pitch + gx);
+#pragma unroll
+    for (int r = 0; r < PF; r++) {
+      const int i = tid + r * kThreads;
+      if (i < TW * TH) tile[i] = pre[r];
     }
     __syncthreads();
     // ---- normalise this thread's window into its A row (pixel m = tid)
@@ -222,6 +240,7 @@ __global__ void __launch_bounds__(kThreads) nn_tc_kernel(const __grid_constant__
       issue_chunk(0, 0);
       if (NCH > 1) issue_chunk(1, 1);
     }
+    prefetch(tile_id + gridDim.x);  // in flight during the epilogue
     // ---- epilogue: lane m of TMEM holds pixel m's pre-activations
     // (softmax branch already in log2 units, Elliott branch as is)
     float wsum = 0.0f, vsum = 0.0f;
