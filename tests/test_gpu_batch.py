@@ -96,3 +96,31 @@ def test_autotuner_picks_and_caches(tmp_path):
     for j, w in zip(jobs, want):
         for o, e in zip(j.outputs, w):
             assert torch.equal(o, e)
+
+
+def test_ragged_random_batches_match_per_frame_launches():
+    """Many small and odd-sized frames of every family in every form: the
+    per-program persistent groups give the per-frame pixels bit for bit."""
+    rng = np.random.default_rng(7)
+    names = ["ravu-lite-r2", "ravu-lite-ar-r3", "ravu-lite-ar-r4", "ravu-r2", "ravu-r3-yuv", "ravu-r4-rgb",
+             "ravu-3x-r2-rgb", "ravu-3x-r4", "ravu-zoom-r2", "ravu-zoom-ar-r2-yuv", "ravu-zoom-r3-rgb",
+             "nnedi3-nns16-win8x4"]
+    jobs = []
+    for i in range(40):
+        name = names[int(rng.integers(len(names)))]
+        hm, _ = synth.model_for(name)
+        H, W = int(rng.integers(1, 40)), int(rng.integers(1, 70))
+        dt = torch.float16 if rng.random() < 0.5 else torch.float32
+        prec = ["fp32", "fast", "mpv"][int(rng.integers(3))]
+        if prec == "mpv":
+            dt = torch.float16
+        osz = (W + int(rng.integers(1, 50)), H + int(rng.integers(1, 30))) if hm.family == "zoom" else None
+        x = torch.from_numpy(synth.frame(H, W, 900 + i, hm.channels)).to("cuda", dt)
+        jobs.append(B.Job.make(hm, x, out_size=osz, precision=prec))
+    want = _expected(jobs)
+    b = B.Batch(jobs)
+    b.launch()
+    torch.cuda.synchronize()
+    for j, w in zip(jobs, want):
+        for o, e in zip(j.outputs, w):
+            assert torch.equal(o, e), (j.model.name, j.precision, tuple(j.inputs[0].shape))
