@@ -134,6 +134,19 @@ const char* pz_last_error(void);
 int pz_model_create(const pz_model_desc* desc, pz_model** out);
 void pz_model_destroy(pz_model* model);
 
+/* What pz_run produces for an input size, so that a host can size its
+ * buffers without knowing the file: output size (2x, 3x, the zoom target or
+ * the enabled NNEDI3 axes), planes per frame and the scratch bytes pz_run
+ * would allocate.  Host-only: no device call. */
+typedef struct {
+  int out_width, out_height;
+  int n_planes;            /* 1 luma, 3 yuv / rgb                            */
+  int family;              /* pz_family                                      */
+  size_t scratch_bytes;    /* as pz_scratch_bytes                            */
+} pz_query_result;
+int pz_query(const pz_model* model, int in_width, int in_height, int dtype, const pz_opts* opts,
+             pz_query_result* out);
+
 /* Device scratch bytes pz_run needs for this model/input (0 if none). */
 size_t pz_scratch_bytes(const pz_model* model, const pz_plane* in, const pz_opts* opts);
 

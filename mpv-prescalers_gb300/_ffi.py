@@ -64,6 +64,11 @@ class Opts(ctypes.Structure):
                 ("scratch", ctypes.c_void_p), ("scratch_bytes", ctypes.c_size_t), ("staging", ctypes.c_int)]
 
 
+class QueryResult(ctypes.Structure):
+    _fields_ = [("out_width", ctypes.c_int), ("out_height", ctypes.c_int), ("n_planes", ctypes.c_int),
+                ("family", ctypes.c_int), ("scratch_bytes", ctypes.c_size_t)]
+
+
 class Job(ctypes.Structure):
     _fields_ = [("model", ctypes.c_void_p), ("inp", Plane * 3), ("out", Plane * 3),
                 ("n_planes", ctypes.c_int), ("opts", Opts)]
@@ -75,6 +80,8 @@ EXPORTS = {
     "pz_model_create": (ctypes.c_int, [ctypes.POINTER(ModelDesc), ctypes.POINTER(ctypes.c_void_p)]),
     "pz_model_destroy": (None, [ctypes.c_void_p]),
     "pz_scratch_bytes": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.POINTER(Plane), ctypes.POINTER(Opts)]),
+    "pz_query": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(Opts),
+                                ctypes.POINTER(QueryResult)]),
     "pz_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Plane), ctypes.c_int, ctypes.POINTER(Plane),
                               ctypes.c_int, ctypes.POINTER(Opts), ctypes.c_void_p]),
     "pz_batch_work_bytes": (ctypes.c_size_t, [ctypes.POINTER(Job), ctypes.c_int]),

@@ -318,6 +318,38 @@ static int nn_axes(const pz_opts* o) {
   return ax == 0 ? 3 : ax;
 }
 
+int pz_query(const pz_model* m, int in_w, int in_h, int dtype, const pz_opts* o, pz_query_result* r) {
+  if (!m || !r) return fail(PZ_EINVAL, "null argument");
+  if (in_w <= 0 || in_h <= 0) return fail(PZ_EINVAL, "bad input size %dx%d", in_w, in_h);
+  if (dtype != PZ_F32 && dtype != PZ_F16) return fail(PZ_EINVAL, "unknown dtype %d", dtype);
+  r->family = m->family;
+  r->n_planes = m->channels == PZ_LUMA ? 1 : 3;
+  r->scratch_bytes = 0;
+  switch (m->family) {
+    case PZ_RAVU_3X:
+      r->out_width = 3 * in_w;
+      r->out_height = 3 * in_h;
+      break;
+    case PZ_RAVU_ZOOM:
+      if (!o || o->out_width <= in_w || o->out_height <= in_h)
+        return fail(PZ_EINVAL, "ravu-zoom needs opts->out_width/out_height above the input size");
+      r->out_width = o->out_width;
+      r->out_height = o->out_height;
+      break;
+    case PZ_NNEDI3: {
+      const int ax = nn_axes(o);
+      r->out_width = (ax & 2) ? 2 * in_w : in_w;
+      r->out_height = (ax & 1) ? 2 * in_h : in_h;
+      if (ax == 3) r->scratch_bytes = (size_t)2 * in_h * in_w * dtype_size(dtype);
+      break;
+    }
+    default:
+      r->out_width = 2 * in_w;
+      r->out_height = 2 * in_h;
+  }
+  return PZ_OK;
+}
+
 size_t pz_scratch_bytes(const pz_model* m, const pz_plane* in, const pz_opts* o) {
   if (!m || !in || m->family != PZ_NNEDI3 || nn_axes(o) != 3) return 0;
   return (size_t)2 * in->height * in->width * dtype_size(in->dtype);

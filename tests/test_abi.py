@@ -68,3 +68,10 @@ def test_resample_arguments_are_checked_on_the_host(lib):
     assert lib.pz_resample(ctypes.byref(a), ctypes.byref(a), float("nan"), 0, 1, 0, 1, None) == _ffi.PZ_EINVAL
     assert lib.pz_resample(ctypes.byref(a), ctypes.byref(a), 1, 0, 1, 3e9, 1, None) == _ffi.PZ_EINVAL
     assert b"out of range" in lib.pz_last_error()
+
+
+def test_query_arguments_are_checked_on_the_host(lib):
+    import ctypes
+    r = _ffi.QueryResult()
+    assert lib.pz_query(None, 8, 8, _ffi.PZ_F16, None, ctypes.byref(r)) == _ffi.PZ_EINVAL
+    assert b"null" in lib.pz_last_error()

@@ -74,3 +74,24 @@ def test_staging_autotuner(tmp_path):
     x = torch.rand((270, 480), device="cuda", dtype=torch.float16)
     best, times = B.autotune_staging(hm, x, cache=B.PlanCache(str(tmp_path / "p.json")), reps=2)
     assert best in ("ldg", "tma") and set(times) == {"ldg", "tma"}
+
+
+@pytest.mark.parametrize("name,osz", [("ravu-lite-ar-r3", None), ("ravu-r3-yuv", None), ("ravu-3x-r2-rgb", None),
+                                      ("ravu-zoom-ar-r2", (101, 77)), ("nnedi3-nns16-win8x4", None),
+                                      ("nnedi3-nns16-win8x4", (40, 60)), ("nnedi3-nns16-win8x4", (80, 30))])
+def test_query_matches_the_python_geometry(name, osz):
+    import ctypes
+    from mpv_prescalers_gb300 import _ffi
+    hm, _ = synth.model_for(name)
+    W, H = 40, 30
+    o = _ffi.Opts()
+    if osz is not None:
+        o.out_width, o.out_height = osz
+    if hm.family == "nnedi3":
+        o.nnedi3_axes = hm.nnedi3_axes(W, H, osz)
+    r = _ffi.QueryResult()
+    _ffi.check(_ffi.lib().pz_query(hm.device_handle(0), W, H, _ffi.PZ_F16, ctypes.byref(o), ctypes.byref(r)))
+    assert (r.out_width, r.out_height) == hm.output_size(W, H, osz)
+    assert r.n_planes == hm.n_planes
+    want_scratch = 2 * W * H * 2 if hm.family == "nnedi3" and o.nnedi3_axes == 3 else 0
+    assert r.scratch_bytes == want_scratch
