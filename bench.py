@@ -238,16 +238,19 @@ def run_gpu(args):
 
     def e2e_step():
         # public API on host frames: H2D copy, upscale and D2H copy of frame i
-        # overlap with its neighbours on three streams
-        for n in MODELS:
-            models[n].upscale_host(host_in, out=host_out[n], precision="fast")
+        # overlap with its neighbours on three streams; both models' calls are
+        # queued before waiting, and the step ends when every frame is back
+        pending = [models[n].upscale_host(host_in, out=host_out[n], precision="fast", wait=False)[1]
+                   for n in MODELS]
+        for ev in pending:
+            ev.synchronize()
 
     for _ in range(args.warmup):
         e2e_step()
     torch.cuda.synchronize()
     barrier()
-    # upscale_host returns when the frames are back in host memory; the two
-    # events on the default stream bracket that wall time
+    # a step returns when the frames are back in host memory; the two events
+    # on the (otherwise idle) default stream bracket that wall time
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -308,6 +311,63 @@ def run_gpu(args):
                            ", FP16 LUT texels, FP32 math"),
                        "batched_mpix_s": res["batched"], "batched_ratio": res["batched"] / res["fp32"],
                        "batched": f"{NFRAMES} FP16 frames per persistent launch, CUDA graph replay"}
+
+    # ---- the other configurations, measured as batches (informational)
+    configs = {}
+    if args.configs:
+        from mpv_prescalers_gb300 import batch as _batch
+        # mixed persistent batch: 16 RGB frames through ravu-zoom-ar-r2-rgb at
+        # 1.5x and at 2.25x, plus 16 4:4:4 YUV frames through ravu-r4-yuv, FP16,
+        # fast form, strategy picked by the autotuner, replayed from a graph
+        zm, _ = synth.model_for("ravu-zoom-ar-r2-rgb")
+        ym, _ = synth.model_for("ravu-r4-yuv")
+        jobs, out_px = [], 0
+        for f in range(16):
+            rgb = torch.from_numpy(synth.rgb_frame(H, W, 4000 + f)).to(dev, torch.float16)
+            yuv = torch.from_numpy(synth.yuv_frame(H, W, 4100 + f)).to(dev, torch.float16)
+            for zr in (1.5, 2.25):
+                osz = (int(W * zr), int(H * zr))
+                jobs.append(_batch.Job.make(zm, rgb, out_size=osz, precision="fast"))
+                out_px += osz[0] * osz[1]
+            jobs.append(_batch.Job.make(ym, yuv, precision="fast"))
+            out_px += 4 * H * W
+        import tempfile
+        ex = _batch.Executor(jobs, cache=_batch.PlanCache(os.path.join(tempfile.mkdtemp(), "plans.json")))
+        for _ in range(2):
+            ex.run()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(3):
+            ex.run()
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / 3
+        configs["zoom_rgb_1.5x_2.25x_plus_ravu_r4_yuv_16_frames_each"] = {
+            "jobs": len(jobs), "ms": ms, "out_mpix_s": out_px / (ms / 1e3) / 1e6, "strategy": ex.strategy,
+            "form": "FP16 planes, fast form"}
+        del ex, jobs
+        # NNEDI3 nns128-win8x6 on 4 frames of 1280x720, fast vs plain FP32
+        nm = models["nnedi3-nns128-win8x6"]
+        res = {}
+        for prec, dt in (("fast", torch.float16), ("fp32", torch.float32)):
+            xs = [torch.from_numpy(synth.luma_plane(720, 1280, 4200 + f)).to(dev, dt) for f in range(4)]
+            ys = [torch.empty((1440, 2560), dtype=dt, device=dev) for _ in range(4)]
+            sc = torch.empty(2 * 720 * 1280 * xs[0].element_size(), dtype=torch.uint8, device=dev)
+            run4 = lambda: [nm.run_raw([x], [y], out_size=(2560, 1440), precision=prec, scratch=sc)
+                            for x, y in zip(xs, ys)]
+            run4()
+            torch.cuda.synchronize()
+            a.record()
+            for _ in range(3):
+                run4()
+            b.record()
+            torch.cuda.synchronize()
+            res[prec] = a.elapsed_time(b) / 3
+        configs["nnedi3_nns128_win8x6_4x1280x720"] = {
+            "fast_ms": res["fast"], "fp32_ms": res["fp32"], "ratio": res["fp32"] / res["fast"],
+            "fast_out_mpix_s": 4 * 2560 * 1440 / (res["fast"] / 1e3) / 1e6}
 
     # ---- serving: Poisson arrivals over 64 streams, mixed resolutions and
     # algorithms (the serving configuration), against serial plain FP32
@@ -370,6 +430,7 @@ def run_gpu(args):
         "clocks": clocks,
         "headline": headline,
         "serving": serving,
+        "other_configs": configs,
         "device": props.name,
     }
     if world > 1:
@@ -460,6 +521,8 @@ def main():
     ap.add_argument("--ref-budget", type=float, default=90.0, help="seconds of CPU work for all reference steps")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=480, help="requests in the serving trace (0: skip)")
+    ap.add_argument("--no-configs", dest="configs", action="store_false",
+                    help="skip the informational batch / NNEDI3 configuration lines")
     args = ap.parse_args()
     if args.case:
         run_case(args.case)

@@ -28,6 +28,29 @@ def test_host_pipeline_matches_device_calls(name):
         assert torch.equal(got[i], ref)
 
 
+def test_host_pipelines_of_two_models_overlap_and_match():
+    """wait=False queues the work and returns an event: two models' host
+    pipelines in flight together give the same frames as device calls."""
+    a, _ = synth.model_for("ravu-lite-ar-r4")
+    b, _ = synth.model_for("nnedi3-nns16-win8x4")
+    frames = torch.stack([torch.from_numpy(synth.luma_plane(30, 44, 300 + i))[None] for i in range(4)])
+    frames = frames.to(torch.float16).pin_memory()
+    ya, ea = a.upscale_host(frames, precision="fast", wait=False)
+    yb, eb = b.upscale_host(frames, precision="fast", wait=False)
+    ea.synchronize()
+    eb.synchronize()
+    for i in range(4):
+        assert torch.equal(ya[i], a.upscale(frames[i].cuda(), precision="fast").cpu())
+        assert torch.equal(yb[i], b.upscale(frames[i].cuda(), precision="fast").cpu())
+
+
+def test_host_pipeline_when_false_passes_frames_through():
+    hm, _ = synth.model_for("ravu-lite-r3")
+    frames = torch.rand((2, 1, 20, 30)).pin_memory()
+    y = hm.upscale_host(frames, out_size=(33, 22))   # below the //!WHEN ratio
+    assert torch.equal(y, frames)
+
+
 def test_batch_of_frames_matches_frame_by_frame():
     hm, _ = synth.model_for("ravu-zoom-ar-r2-rgb")
     x = torch.stack([torch.from_numpy(synth.rgb_frame(30, 40, 7 + i)) for i in range(3)]).cuda()
