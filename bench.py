@@ -379,11 +379,17 @@ def run_gpu(args):
         serve.Server(smodels).run(serve.warmup_trace(smodels))
         srv = serve.Server(smodels, hbm_budget=40e9, slots=8)
         served = srv.run(trace)
+        # the same trace with each stream's output frames owned by the caller
+        # (a ring of 3 pinned buffers per stream) instead of one host
+        # allocation per request
+        ring_trace = serve.poisson_trace(smodels, args.serve_requests, rate=240.0, streams=64, frame_pool=1,
+                                         out_ring=3)
+        served_ring = serve.Server(smodels, hbm_budget=40e9, slots=8).run(ring_trace)
         serial = serve.serial_baseline(smodels, trace)
         serving = {"trace": f"{len(trace)} requests, Poisson 240 frames/s over 64 streams, resolutions "
                             "{480p .3, 720p .3, 1080p .3, 2160p .1}, algorithms {ravu-lite-ar-r3, ravu-r4-yuv, "
                             "nnedi3-nns64-win8x4, ravu-zoom-ar-r2 at 1.75x}, FP16 planes, 40 GB budget",
-                   "served": served, "serial_fp32": serial}
+                   "served": served, "served_caller_buffers": served_ring, "serial_fp32": serial}
 
     props = torch.cuda.get_device_properties(dev)
     clocks = clk.summary()

@@ -54,6 +54,8 @@ class Request:
     # filled in by the server
     admit: float = -1.0
     finish: float = -1.0
+    # the host frame the result lands in: the caller's pinned buffer of the
+    # output's shape when given (a player's own frame buffer), else allocated
     output: Optional["torch.Tensor"] = None
 
     @property
@@ -138,7 +140,9 @@ class Server:
             for r, job in zip(reqs, jobs):
                 o0 = job.outputs[0]
                 out = o0.as_strided((len(job.outputs),) + tuple(o0.shape), (o0.numel(),) + tuple(o0.stride()))
-                r.output = torch.empty(out.shape, dtype=out.dtype, pin_memory=True)
+                if not (r.output is not None and tuple(r.output.shape) == tuple(out.shape)
+                        and r.output.dtype == out.dtype and r.output.is_pinned()):
+                    r.output = torch.empty(out.shape, dtype=out.dtype, pin_memory=True)
                 r.output.copy_(out, non_blocking=True)
             slot.done = torch.cuda.Event(enable_timing=True)
             slot.done.record(slot.stream)
@@ -206,14 +210,24 @@ def serial_baseline(models: Dict[str, HookModel], trace: Sequence[Request]) -> D
     dev = torch.device("cuda", torch.cuda.current_device())
     clock = 0.0
     done = []
-    for r in sorted(trace, key=lambda q: q.arrival):
-        q = Request(r.rid, r.stream_id, r.model, r.frame.float(), r.arrival, r.out_size, "fp32")
+    host_out: Dict[Tuple, "torch.Tensor"] = {}   # one pinned result buffer per shape, made before timing
+    reqs = [Request(r.rid, r.stream_id, r.model, _pinned(r.frame.float()), r.arrival, r.out_size, "fp32")
+            for r in sorted(trace, key=lambda q: q.arrival)]
+    for q in reqs:
+        m = models[q.model]
+        C, H, W = q.frame.shape
+        OW, OH = m.output_size(W, H, q.out_size)
+        key = (C, OH, OW)
+        if key not in host_out:
+            host_out[key] = _pinned(torch.empty(key, dtype=torch.float32))
+    for q in reqs:
         start = max(clock, q.arrival)
         torch.cuda.synchronize(dev)
         t = time.perf_counter()
-        xd = q.frame.to(dev)
+        xd = q.frame.to(dev, non_blocking=True)
         y = models[q.model].upscale(xd, out_size=q.out_size, precision="fp32")
-        q.output = y.cpu()
+        q.output = host_out[tuple(y.shape)]
+        q.output.copy_(y, non_blocking=True)
         torch.cuda.synchronize(dev)
         clock = start + (time.perf_counter() - t)
         q.finish = clock
@@ -247,10 +261,13 @@ def warmup_trace(models: Dict[str, HookModel], resolutions=RESOLUTIONS, algorith
 
 def poisson_trace(models: Dict[str, HookModel], n: int, rate: float = 240.0, streams: int = 64,
                   seed: int = 5000, precision: str = "fast", frame_pool: int = 2,
-                  resolutions=RESOLUTIONS, algorithms=ALGORITHMS) -> List[Request]:
+                  resolutions=RESOLUTIONS, algorithms=ALGORITHMS, out_ring: int = 0) -> List[Request]:
     """Poisson arrivals at `rate` frames/s over `streams` streams; resolution
     and algorithm drawn per stream (the mix of the serving configuration).
-    Frames come from a small pool of seeded synthetic frames per resolution."""
+    Frames come from a small pool of seeded synthetic frames per resolution.
+    ``out_ring`` > 0 gives every stream that many pinned output frames,
+    reused in turn (a player's own frame buffers); 0 lets the server
+    allocate one per request."""
     from . import synth
     torch = _torch()
     rng = np.random.default_rng(seed)
@@ -269,6 +286,8 @@ def poisson_trace(models: Dict[str, HookModel], n: int, rate: float = 240.0, str
 
     t = 0.0
     out = []
+    rings: Dict[int, list] = {}
+    counts: Dict[int, int] = {}
     for rid in range(n):
         t += rng.exponential(1.0 / rate)
         sid = int(rng.integers(0, streams))
@@ -277,5 +296,13 @@ def poisson_trace(models: Dict[str, HookModel], n: int, rate: float = 240.0, str
         m = models[name]
         f = frame(int(stream_res[sid]), m.channels, rid)
         osz = (int(round(W * zoom)), int(round(H * zoom))) if zoom else None
-        out.append(Request(rid, sid, name, f, t, osz, precision))
+        r = Request(rid, sid, name, f, t, osz, precision)
+        if out_ring > 0:
+            OW, OH = m.output_size(W, H, osz)
+            ring = rings.setdefault(sid, [])
+            if len(ring) < out_ring:
+                ring.append(_pinned(torch.empty((m.n_planes, OH, OW), dtype=torch.float16)))
+            r.output = ring[counts.get(sid, 0) % out_ring]
+            counts[sid] = counts.get(sid, 0) + 1
+        out.append(r)
     return out

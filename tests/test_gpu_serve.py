@@ -17,15 +17,21 @@ def models():
     return {name: synth.model_for(name)[0] for name, _ in serve.ALGORITHMS}
 
 
-@pytest.mark.parametrize("mode", ["streams", "batch"])
-def test_each_result_same_alone_and_in_the_mix(models, mode):
-    trace = serve.poisson_trace(models, 48, rate=4000.0, streams=12, seed=11, resolutions=SMALL, frame_pool=2)
+@pytest.mark.parametrize("mode,ring", [("streams", 0), ("batch", 0), ("streams", 64)])
+def test_each_result_same_alone_and_in_the_mix(models, mode, ring):
+    """ring > 0: the results land in caller-owned pinned frames (enough per
+    stream that none is reused within the trace)."""
+    trace = serve.poisson_trace(models, 48, rate=4000.0, streams=12, seed=11, resolutions=SMALL, frame_pool=2,
+                                out_ring=ring)
+    given = [r.output for r in trace]
     srv = serve.Server(models, hbm_budget=40e9, slots=6, mode=mode)
     stats = srv.run(trace)
     assert stats["requests"] == len(trace)
     for r in trace:
         alone = models[r.model].upscale(r.frame.cuda(), out_size=r.out_size, precision=r.precision).cpu()
         assert r.output is not None and torch.equal(r.output, alone), (r.rid, r.model)
+    if ring:
+        assert all(r.output is g for r, g in zip(trace, given))   # written in place
     assert stats["p99_ms"] >= stats["p50_ms"] > 0
 
 

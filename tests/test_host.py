@@ -205,3 +205,21 @@ def test_bench_replica_timing_single_process():
     import bench
     assert bench.max_over_ranks(3.25) == 3.25
     assert bench.job_value(2e6, 10, 1000.0, 1) == pytest.approx(20.0)
+
+
+def test_trace_output_rings_are_per_stream_and_shaped():
+    models = _trace_models()
+    res = ((64, 36, 0.5), (96, 54, 0.5))
+    t = S.poisson_trace(models, 200, rate=200.0, streams=8, seed=3, resolutions=res, out_ring=3)
+    by_stream = {}
+    for r in t:
+        m = models[r.model]
+        h, w = r.frame.shape[-2:]
+        ow, oh = m.output_size(w, h, r.out_size)
+        assert tuple(r.output.shape) == (m.n_planes, oh, ow)
+        by_stream.setdefault(r.stream_id, []).append(r.output)
+    for outs in by_stream.values():
+        assert len({o.data_ptr() for o in outs}) == min(3, len(outs))
+        for i in range(3, len(outs)):
+            assert outs[i] is outs[i - 3]
+    assert all(r.output is None for r in S.poisson_trace(models, 20, resolutions=res, seed=3))
