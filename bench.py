@@ -491,6 +491,10 @@ CASES = {
     "ravu-zoom-ar-r2-rgb-fast": ("ravu-zoom-ar-r2-rgb", (2880, 1620), "fast"),
     "nnedi3-nns128-win8x6-fast": ("nnedi3-nns128-win8x6", None, "fast"),
     "nnedi3-nns128-win8x6-fp32": ("nnedi3-nns128-win8x6", None, "fp32"),
+    # not a model: the OFFSET correction of a 3840x2160 FP16 plane (pz_resample,
+    # Catmull-Rom), and a persistent batch of 8 1080p ravu-lite-ar-r4 frames
+    "resample-2160p": (None, None, None),
+    "batch-ravu-lite-ar-r4-8x1080p": ("ravu-lite-ar-r4", None, "fast"),
 }
 
 
@@ -500,16 +504,31 @@ def run_case(name: str) -> None:
     _pkg()
     from mpv_prescalers_gb300 import synth
     model, out_size, prec = CASES[name]
-    hm, src = synth.model_for(model)
-    x = torch.from_numpy(synth.frame(H, W, SEED0, hm.channels)).to("cuda", torch.float16)
+    src = "n/a"
+    if name == "resample-2160p":
+        from mpv_prescalers_gb300 import frame as _frame
+        y = torch.from_numpy(synth.luma_plane(2 * H, 2 * W, SEED0)).to("cuda", torch.float16)
+        o = torch.empty_like(y)
+        call = lambda: _frame.resample_plane(y, 2 * W, 2 * H, 1.0, -0.5, 1.0, -0.5, "catmull_rom", out=o)
+    elif name.startswith("batch-"):
+        from mpv_prescalers_gb300 import batch as _batch
+        hm, src = synth.model_for(model)
+        jobs = [_batch.Job.make(hm, torch.from_numpy(synth.luma_plane(H, W, SEED0 + f)).to("cuda", torch.float16),
+                                precision=prec) for f in range(NFRAMES)]
+        plan = _batch.Batch(jobs)
+        call = plan.launch
+    else:
+        hm, src = synth.model_for(model)
+        x = torch.from_numpy(synth.frame(H, W, SEED0, hm.channels)).to("cuda", torch.float16)
+        call = lambda: hm.upscale(x, out_size=out_size, precision=prec)
     for _ in range(3):
-        hm.upscale(x, out_size=out_size, precision=prec)
+        call()
     torch.cuda.synchronize()
     a = torch.cuda.Event(enable_timing=True)
     b = torch.cuda.Event(enable_timing=True)
     a.record()
     for _ in range(3):
-        hm.upscale(x, out_size=out_size, precision=prec)
+        call()
     b.record()
     torch.cuda.synchronize()
     print(json.dumps({"case": name, "weights": src, "ms_per_call": a.elapsed_time(b) / 3}))
