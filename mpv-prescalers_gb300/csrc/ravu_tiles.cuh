@@ -724,36 +724,47 @@ __global__ void __launch_bounds__(kTileThreads) persistent_kernel(const DevJob* 
   extern __shared__ __align__(128) float4 psmem[];
   float* smem = reinterpret_cast<float*>(psmem);
   __shared__ RavuArgs s_args;
-  __shared__ int s_item, s_job, s_tw, s_first;
+  // claim slots alternate between iterations: thread 0 fills slot (i+1)&1
+  // while the other threads may still read slot i&1, and cannot get two
+  // iterations ahead (the claim barrier of iteration i+1 holds it)
+  __shared__ int s_item[2], s_job[2], s_tw[2], s_first[2];
   int loaded = -1;
-  for (;;) {
+  // thread 0 claims the next tile while the current one runs
+  int next = threadIdx.x == 0 ? atomicAdd(counter, 1) : 0;
+  for (int it = 0;; it ^= 1) {
     if (threadIdx.x == 0) {
-      const int item = atomicAdd(counter, 1);
-      s_item = item;
+      const int item = next;
+      s_item[it] = item;
       if (item < total) {
-        int lo = 0, hi = n_jobs - 1;
+        next = atomicAdd(counter, 1);
+        int lo = 0, hi = n_jobs - 1;  // last job whose first tile <= item
         while (lo < hi) {
           const int mid = (lo + hi + 1) >> 1;
           if (jobs[mid].first_tile <= item) lo = mid; else hi = mid - 1;
         }
-        s_job = lo;
-        s_tw = jobs[lo].tiles_w;
-        s_first = jobs[lo].first_tile;
+        s_job[it] = lo;
+        s_tw[it] = jobs[lo].tiles_w;
+        s_first[it] = jobs[lo].first_tile;
       }
     }
     __syncthreads();
-    const int item = s_item;
+    const int item = s_item[it];
     if (item >= total) break;
-    if (s_job != loaded) {  // uniform: every thread reads the same s_job
-      loaded = s_job;
+    const int job = s_job[it], tw = s_tw[it], first = s_first[it];
+    if (job != loaded) {  // uniform: every thread reads the same slot
+      // every thread is past the previous tile (the claim barrier above), so
+      // s_args is free
+      loaded = job;
       const int* src = reinterpret_cast<const int*>(&jobs[loaded].a);
       int* dst = reinterpret_cast<int*>(&s_args);
       for (int i = threadIdx.x; i < (int)(sizeof(RavuArgs) / 4); i += kTileThreads) dst[i] = src[i];
       __syncthreads();
     }
-    const int t = item - s_first;
-    Prog::run(s_args, (t % s_tw) * kTileW, (t / s_tw) * kTileH, smem, nullptr);
-    __syncthreads();  // the tile's shared memory and s_item are free for the next claim
+    const int t = item - first;
+    // No barrier after the tile: the next tile's staging and argument copy
+    // come after the next claim barrier, which every thread reaches only
+    // when done with this tile.
+    Prog::run(s_args, (t % tw) * kTileW, (t / tw) * kTileH, smem, nullptr);
   }
 }
 

@@ -12,8 +12,9 @@
 //   u = sx * x + ox,  v = sy * y + oy,
 // with texel centres at integer coordinates and clamp-to-edge borders.
 // k is the bilinear tent or the Catmull-Rom cubic (Keys' cubic convolution
-// kernel with a = -1/2).  The kernel is bound by the output write: one
-// thread per output texel, the 2x2 or 4x4 input footprint comes from L1.
+// kernel with a = -1/2).  One thread per output texel; the 2x2 or 4x4 input
+// footprint comes through L1 (a variant staging each block's footprint in
+// shared memory first measured 10 % slower).
 #include "../../include/prescale.h"
 #include "kernels.h"
 #include "model.h"
@@ -44,7 +45,7 @@ __global__ void __launch_bounds__(256) resample_kernel(const ResampleArgs a) {
   const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
   if (x >= a.out_w || y >= a.out_h) return;
   const T* in = static_cast<const T*>(a.in);
-  const float u = a.sx * (float)x + a.ox, v = a.sy * (float)y + a.oy;
+  const float u = fmaf(a.sx, (float)x, a.ox), v = fmaf(a.sy, (float)y, a.oy);
   const float fu = floorf(u), fv = floorf(v);
   const int iu = (int)fu, iv = (int)fv;
   float wx[4], wy[4];
