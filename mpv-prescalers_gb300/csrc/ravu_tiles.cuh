@@ -157,6 +157,9 @@ struct LiteTile {
   static constexpr size_t smem_bytes = (size_t)((TW * TH + 3) & ~3) * 4;
 
   static constexpr int kPlanes = 1;
+  // ravu-lite-ar-r4 fits 5 CTAs per SM at <= 48 registers (measured 2 %
+  // faster); the other radii lose more to spills than they gain
+  static constexpr int kMinBlocks = (R == 4 && AR) ? 5 : 1;
   using Elem = T;
 
   __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, const TmaCtx* tma = nullptr) {
@@ -252,6 +255,7 @@ struct ThreeXTile {
   static constexpr int C = CM == kLuma ? 1 : 3;
   static constexpr size_t smem_bytes = (size_t)(C + (CM == kRgb ? 1 : 0)) * TW * TH * 4;
   static constexpr int kPlanes = C;
+  static constexpr int kMinBlocks = 1;
   using Elem = T;
 
   __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, const TmaCtx* tma = nullptr) {
@@ -378,6 +382,7 @@ struct Int11Tile {
   static constexpr int C = CM == kLuma ? 1 : 3;
   static constexpr size_t smem_bytes = (size_t)(C + (CM == kRgb ? 1 : 0)) * TW * TH * 4;
   static constexpr int kPlanes = C;
+  static constexpr int kMinBlocks = 1;
   using Elem = T;
 
   __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, const TmaCtx* tma = nullptr) {
@@ -441,6 +446,7 @@ struct LatticeTile {
   static constexpr int PL = C + (CM == kRgb ? 1 : 0);  // planes per tile set
   static constexpr size_t smem_bytes = (size_t)2 * PL * TW * TH * 4;
   static constexpr int kPlanes = C;
+  static constexpr int kMinBlocks = 1;
   using Elem = T;
 
   __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, const TmaCtx* tma = nullptr) {
@@ -555,6 +561,7 @@ struct ZoomTile {
   static constexpr size_t smem_bytes = (size_t)(C + (CM == kRgb ? 1 : 0)) * RW * RH * 4;
 
   static constexpr int kPlanes = 0;  // the input rectangle moves with the ratio: clamped loads only
+  static constexpr int kMinBlocks = 1;
   using Elem = T;
 
   __device__ static void run(const RavuArgs& p, int X0, int Y0, float* smem, const TmaCtx* = nullptr) {
@@ -646,7 +653,7 @@ struct ZoomTile {
 // One CTA per tile of a single frame; with TMA the frame tile of interior
 // tiles comes in by cp.async.bulk.tensor.
 template <class Prog, bool TMA>
-__global__ void __launch_bounds__(kTileThreads) tile_kernel(const __grid_constant__ RavuArgs p,
+__global__ void __launch_bounds__(kTileThreads, Prog::kMinBlocks) tile_kernel(const __grid_constant__ RavuArgs p,
                                                             const __grid_constant__ TmaMaps maps) {
   extern __shared__ __align__(128) float4 tile_smem[];
   float* smem = reinterpret_cast<float*>(tile_smem);
@@ -719,7 +726,7 @@ struct DevJob {
 // copied to shared memory when the job changes.  Every job of a launch runs
 // the same program, so register use and shared memory are the program's own.
 template <class Prog>
-__global__ void __launch_bounds__(kTileThreads) persistent_kernel(const DevJob* __restrict__ jobs, int n_jobs,
+__global__ void __launch_bounds__(kTileThreads, Prog::kMinBlocks) persistent_kernel(const DevJob* __restrict__ jobs, int n_jobs,
                                                                   int total, int* counter) {
   extern __shared__ __align__(128) float4 psmem[];
   float* smem = reinterpret_cast<float*>(psmem);

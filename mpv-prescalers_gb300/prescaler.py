@@ -277,6 +277,8 @@ class HookModel:
         if len(pl) != self.n_planes:
             raise ValueError(f"{self.name} takes {self.n_planes} plane(s), got {len(pl)}")
         H, W = pl[0].shape
+        if H == 0 or W == 0:
+            raise ValueError(f"empty plane {W}x{H}")
         for p in pl:
             if not p.is_cuda:
                 raise ValueError("planes must be CUDA tensors")

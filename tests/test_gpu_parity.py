@@ -280,3 +280,31 @@ def test_bad_arguments_raise():
         lite.run_raw([x], [torch.empty((41, 60), device="cuda")], out_size=(60, 41))  # wrong size
     with pytest.raises(ValueError):
         lite.upscale(torch.rand((3, 20, 30), device="cuda"))  # lite is luma only
+
+
+@pytest.mark.parametrize("name", ["ravu-lite-ar-r3", "ravu-r3", "nnedi3-nns16-win8x4"])
+def test_largest_frame_crop_matches_the_oracle(name):
+    """A 3840x2160 input (the largest frame of the serving mix) in the fast
+    form: a block of the output, away from the frame border, equals the
+    oracle run on the matching input crop (the output at a pixel depends on
+    its window only), to the FP16 bar."""
+    hm = _model(name)
+    x = synth.luma_plane(2160, 3840, 93).astype(np.float16).astype(np.float32)
+    y = hm.upscale(torch.from_numpy(x).to("cuda", torch.float16), precision="fast").float().cpu().numpy()
+    y0, x0, h, w, m = 1500, 3100, 24, 40, 6   # crop origin, size, margin beyond the window reach
+    crop = x[y0 - m:y0 + h + m, x0 - m:x0 + w + m]
+    if hm.family == "nnedi3":
+        ref, _ = oracle.nnedi3_upscale(hm.model, crop)
+    else:
+        ref, _ = oracle.keyed_upscale(hm.model, crop[None], (2 * crop.shape[1], 2 * crop.shape[0]))
+    ref = np.asarray(ref).reshape(2 * crop.shape[0], 2 * crop.shape[1])[2 * m:-2 * m, 2 * m:-2 * m]
+    got = y.reshape(2 * 2160, 2 * 3840)[2 * y0:2 * (y0 + h), 2 * x0:2 * (x0 + w)]
+    assert np.abs(got - ref).max() <= TOL_FP16_MAXABS or _psnr(got, ref) >= TOL_FP16_PSNR + 10
+
+
+def test_empty_planes_are_rejected():
+    from mpv_prescalers_gb300 import PrescaleError
+    hm = _model("ravu-lite-r2")
+    x = torch.empty((0, 30), device="cuda")
+    with pytest.raises((PrescaleError, ValueError)):
+        hm.upscale(x)
