@@ -159,7 +159,7 @@ struct LiteTile {
   static constexpr int kPlanes = 1;
   // ravu-lite-ar-r4 fits 5 CTAs per SM at <= 48 registers (measured 2 %
   // faster); the other radii lose more to spills than they gain
-  static constexpr int kMinBlocks = (R == 4 && AR) ? 5 : 1;
+  static constexpr int kMinBlocks = (R == 4 && AR) ? 5 : 0;
   using Elem = T;
 
   __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, const TmaCtx* tma = nullptr) {
@@ -255,7 +255,7 @@ struct ThreeXTile {
   static constexpr int C = CM == kLuma ? 1 : 3;
   static constexpr size_t smem_bytes = (size_t)(C + (CM == kRgb ? 1 : 0)) * TW * TH * 4;
   static constexpr int kPlanes = C;
-  static constexpr int kMinBlocks = 1;
+  static constexpr int kMinBlocks = 0;  // no launch-bounds minimum
   using Elem = T;
 
   __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, const TmaCtx* tma = nullptr) {
@@ -382,7 +382,7 @@ struct Int11Tile {
   static constexpr int C = CM == kLuma ? 1 : 3;
   static constexpr size_t smem_bytes = (size_t)(C + (CM == kRgb ? 1 : 0)) * TW * TH * 4;
   static constexpr int kPlanes = C;
-  static constexpr int kMinBlocks = 1;
+  static constexpr int kMinBlocks = 0;  // no launch-bounds minimum
   using Elem = T;
 
   __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, const TmaCtx* tma = nullptr) {
@@ -446,7 +446,7 @@ struct LatticeTile {
   static constexpr int PL = C + (CM == kRgb ? 1 : 0);  // planes per tile set
   static constexpr size_t smem_bytes = (size_t)2 * PL * TW * TH * 4;
   static constexpr int kPlanes = C;
-  static constexpr int kMinBlocks = 1;
+  static constexpr int kMinBlocks = 0;  // no launch-bounds minimum
   using Elem = T;
 
   __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, const TmaCtx* tma = nullptr) {
@@ -561,7 +561,7 @@ struct ZoomTile {
   static constexpr size_t smem_bytes = (size_t)(C + (CM == kRgb ? 1 : 0)) * RW * RH * 4;
 
   static constexpr int kPlanes = 0;  // the input rectangle moves with the ratio: clamped loads only
-  static constexpr int kMinBlocks = 1;
+  static constexpr int kMinBlocks = 0;  // no launch-bounds minimum
   using Elem = T;
 
   __device__ static void run(const RavuArgs& p, int X0, int Y0, float* smem, const TmaCtx* = nullptr) {
@@ -653,8 +653,7 @@ struct ZoomTile {
 // One CTA per tile of a single frame; with TMA the frame tile of interior
 // tiles comes in by cp.async.bulk.tensor.
 template <class Prog, bool TMA>
-__global__ void __launch_bounds__(kTileThreads, Prog::kMinBlocks) tile_kernel(const __grid_constant__ RavuArgs p,
-                                                            const __grid_constant__ TmaMaps maps) {
+__device__ __forceinline__ void tile_body(const RavuArgs& p, const TmaMaps& maps) {
   extern __shared__ __align__(128) float4 tile_smem[];
   float* smem = reinterpret_cast<float*>(tile_smem);
   if (TMA) {
@@ -667,6 +666,27 @@ __global__ void __launch_bounds__(kTileThreads, Prog::kMinBlocks) tile_kernel(co
   } else {
     Prog::run(p, blockIdx.x * kTileW, blockIdx.y * kTileH, smem, nullptr);
   }
+}
+
+// Programs with kMinBlocks > 0 ask the compiler for that many resident CTAs
+// per SM (a register cap); the others keep the compiler's own allocation.
+template <class Prog, bool TMA>
+__global__ void __launch_bounds__(kTileThreads) tile_kernel(const __grid_constant__ RavuArgs p,
+                                                            const __grid_constant__ TmaMaps maps) {
+  tile_body<Prog, TMA>(p, maps);
+}
+template <class Prog, bool TMA>
+__global__ void __launch_bounds__(kTileThreads, Prog::kMinBlocks) tile_kernel_mb(const __grid_constant__ RavuArgs p,
+                                                                               const __grid_constant__ TmaMaps maps) {
+  tile_body<Prog, TMA>(p, maps);
+}
+
+template <class Prog, bool TMA>
+void launch_tile_kernel(dim3 grid, size_t smem, cudaStream_t s, const RavuArgs& a, const TmaMaps& maps) {
+  if constexpr (Prog::kMinBlocks > 0)
+    tile_kernel_mb<Prog, TMA><<<grid, kTileThreads, smem, s>>>(a, maps);
+  else
+    tile_kernel<Prog, TMA><<<grid, kTileThreads, smem, s>>>(a, maps);
 }
 
 bool encode_plane_map(CUtensorMap* map, const void* base, int W, int H, int pitch, int dtype, int box_w,
@@ -688,12 +708,12 @@ int launch_tiles(const RavuArgs& a, int tiles_w, int tiles_h, cudaStream_t s) {
         constexpr size_t smem = ((Prog::smem_bytes + 127) & ~(size_t)127) +
                                 (size_t)Prog::kPlanes * tma_plane_bytes<Prog::TW, Prog::TH, typename Prog::Elem>();
         static_assert(smem <= 48 * 1024, "TMA staging needs more than the default shared memory");
-        tile_kernel<Prog, true><<<dim3(tiles_w, tiles_h), kTileThreads, smem, s>>>(a, maps);
+        launch_tile_kernel<Prog, true>(dim3(tiles_w, tiles_h), smem, s, a, maps);
         return 0;
       }
     }
   }
-  tile_kernel<Prog, false><<<dim3(tiles_w, tiles_h), kTileThreads, Prog::smem_bytes, s>>>(a, maps);
+  launch_tile_kernel<Prog, false>(dim3(tiles_w, tiles_h), Prog::smem_bytes, s, a, maps);
   return 0;
 }
 
@@ -726,8 +746,8 @@ struct DevJob {
 // copied to shared memory when the job changes.  Every job of a launch runs
 // the same program, so register use and shared memory are the program's own.
 template <class Prog>
-__global__ void __launch_bounds__(kTileThreads, Prog::kMinBlocks) persistent_kernel(const DevJob* __restrict__ jobs, int n_jobs,
-                                                                  int total, int* counter) {
+__device__ __forceinline__ void persistent_body(const DevJob* __restrict__ jobs, int n_jobs, int total,
+                                                int* counter) {
   extern __shared__ __align__(128) float4 psmem[];
   float* smem = reinterpret_cast<float*>(psmem);
   __shared__ RavuArgs s_args;
@@ -775,6 +795,17 @@ __global__ void __launch_bounds__(kTileThreads, Prog::kMinBlocks) persistent_ker
   }
 }
 
+template <class Prog>
+__global__ void __launch_bounds__(kTileThreads) persistent_kernel(const DevJob* __restrict__ jobs, int n_jobs,
+                                                                  int total, int* counter) {
+  persistent_body<Prog>(jobs, n_jobs, total, counter);
+}
+template <class Prog>
+__global__ void __launch_bounds__(kTileThreads, Prog::kMinBlocks) persistent_kernel_mb(
+    const DevJob* __restrict__ jobs, int n_jobs, int total, int* counter) {
+  persistent_body<Prog>(jobs, n_jobs, total, counter);
+}
+
 // Launch and occupancy query of one program's persistent kernel.
 struct PersistentOps {
   void (*launch)(const DevJob* jobs, int n_jobs, int total, int* counter, int grid, cudaStream_t s);
@@ -784,15 +815,27 @@ struct PersistentOps {
 template <class Prog>
 PersistentOps persistent_ops() {
   static_assert(Prog::smem_bytes <= 48 * 1024, "tile program needs more than the default shared memory");
-  return {[](const DevJob* j, int n, int total, int* c, int grid, cudaStream_t s) {
-            persistent_kernel<Prog><<<grid, kTileThreads, Prog::smem_bytes, s>>>(j, n, total, c);
-          },
-          []() {
-            int fit = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, persistent_kernel<Prog>, kTileThreads,
-                                                          Prog::smem_bytes);
-            return fit;
-          }};
+  if constexpr (Prog::kMinBlocks > 0) {
+    return {[](const DevJob* j, int n, int total, int* c, int grid, cudaStream_t s) {
+              persistent_kernel_mb<Prog><<<grid, kTileThreads, Prog::smem_bytes, s>>>(j, n, total, c);
+            },
+            []() {
+              int fit = 0;
+              cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, persistent_kernel_mb<Prog>, kTileThreads,
+                                                            Prog::smem_bytes);
+              return fit;
+            }};
+  } else {
+    return {[](const DevJob* j, int n, int total, int* c, int grid, cudaStream_t s) {
+              persistent_kernel<Prog><<<grid, kTileThreads, Prog::smem_bytes, s>>>(j, n, total, c);
+            },
+            []() {
+              int fit = 0;
+              cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, persistent_kernel<Prog>, kTileThreads,
+                                                            Prog::smem_bytes);
+              return fit;
+            }};
+  }
 }
 
 // The ops of program `prog` for plane dtype `dtype` (0 FP32, 1 FP16), or
