@@ -96,13 +96,44 @@ __device__ __forceinline__ float sqrt_approx(float x) {
   return r;
 }
 
+// floor(24 * theta / pi) with theta = mod(atan(y, x) + pi, pi) in [0, pi),
+// without the arctangent: the direction is folded into [0, pi/4] (a turn by
+// -pi/2, then a mirror about the diagonal) and the sector boundaries
+// k*pi/24 below it are counted by comparing y with tan(k*pi/24) * x.  Only
+// directions within FP32 rounding of a boundary can land in the neighbouring
+// sector (the oracle's boundary keys); a NaN component gives sector 0.
+__device__ __forceinline__ float angle_sector(float x, float y) {
+  if (y < 0.0f || (y == 0.0f && x < 0.0f)) {  // theta + pi: same direction mod pi
+    x = -x;
+    y = -y;
+  }
+  float base = 0.0f;
+  if (x < 0.0f) {  // theta in (pi/2, pi): turn by -pi/2
+    const float t = x;
+    x = y;
+    y = -t;
+    base = 12.0f;
+  }
+  const bool mirror = y > x;  // above pi/4: theta'' = pi/2 - theta'
+  if (mirror) {
+    const float t = x;
+    x = y;
+    y = t;
+  }
+  const float s = (float)((int)(y >= 0.131652498f * x) + (int)(y >= 0.267949192f * x) +
+                          (int)(y >= 0.414213562f * x) + (int)(y >= 0.577350269f * x) +
+                          (int)(y >= 0.767326988f * x) + (int)(y >= x));
+  return base + (mirror ? 11.0f - s : s);
+}
+
 // Eigen analysis + quantisation -> raw key (not clamped to the LUT).
 // ravu-lite-r3.hook:77-88 (strength thresholds), ravu-r3.hook:121-125 (log2).
 //
 // The quantised outputs equal the shader's; only the way each threshold test
 // is evaluated changes, so results can differ only where a quantity lies
 // within FP32 rounding of a threshold (the oracle's boundary keys):
-//   * angle: theta * (24/pi) instead of theta * 24 / pi;
+//   * angle: the sector by comparisons with tan(k*pi/24) (angle_sector)
+//     instead of floor(atan(.) * 24 / pi);
 //   * coherence: mu >= c  <=>  (sqrtL1 - sqrtL2) >= c * (sqrtL1 + sqrtL2),
 //     no division; NaN (L2 < 0) still fails every test -> 0, and the
 //     sqrtL1 + sqrtL2 < eps gate still forces 0;
@@ -112,13 +143,7 @@ __device__ __forceinline__ int ravu_key(float a, float b, float d, const KeyPara
   float delta = sqrt_approx(fmaxf(T * T * 0.25f - D, 0.0f));
   float L1 = T * 0.5f + delta, L2 = T * 0.5f - delta;
   float sqrtL1 = sqrt_approx(L1), sqrtL2 = sqrt_approx(L2);
-  float theta = 0.0f;
-  if (!(fabsf(b) < kFltEps)) {
-    theta = atan2f(L1 - a, b) + kPi;  // mod(atan(L1 - a, b) + pi, pi), t in [0, 2pi]
-    theta = theta >= kPi ? theta - kPi : theta;
-    theta = theta >= kPi ? theta - kPi : theta;  // t = 2pi exactly -> 0, as mod() gives
-  }
-  float angle = floorf(theta * (24.0f / kPi));
+  const float angle = fabsf(b) < kFltEps ? 0.0f : angle_sector(b, L1 - a);
   float lambda = sqrtL1;
   float strength;
   if (kp.log2_mode) {

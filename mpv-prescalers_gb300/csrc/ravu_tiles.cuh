@@ -382,7 +382,9 @@ struct Int11Tile {
   static constexpr int C = CM == kLuma ? 1 : 3;
   static constexpr size_t smem_bytes = (size_t)(C + (CM == kRgb ? 1 : 0)) * TW * TH * 4;
   static constexpr int kPlanes = C;
-  static constexpr int kMinBlocks = 0;  // no launch-bounds minimum
+  // register caps measured best on GB300: r3 8 CTAs per SM, r4 5, r2 the
+  // compiler's own allocation
+  static constexpr int kMinBlocks = R == 3 ? 8 : (R == 4 ? 5 : 0);
   using Elem = T;
 
   __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, const TmaCtx* tma = nullptr) {
@@ -446,7 +448,9 @@ struct LatticeTile {
   static constexpr int PL = C + (CM == kRgb ? 1 : 0);  // planes per tile set
   static constexpr size_t smem_bytes = (size_t)2 * PL * TW * TH * 4;
   static constexpr int kPlanes = C;
-  static constexpr int kMinBlocks = 0;  // no launch-bounds minimum
+  // register caps measured best on GB300: r3 5 CTAs per SM, r4 3, r2 the
+  // compiler's own allocation
+  static constexpr int kMinBlocks = R == 3 ? 5 : (R == 4 ? 3 : 0);
   using Elem = T;
 
   __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, const TmaCtx* tma = nullptr) {
