@@ -157,6 +157,27 @@ size_t pz_scratch_bytes(const pz_model* model, const pz_plane* in, const pz_opts
 int pz_run(const pz_model* model, const pz_plane* in, int n_in, pz_plane* out, int n_out,
            const pz_opts* opts, void* cuda_stream);
 
+/* ---- frames in host memory --------------------------------------------
+ * For hosts that decode in software and hold frames in host memory: runs
+ * the chain over n_frames frames, copying frame i in, running it and copying
+ * it back while its neighbours' transfers run under its kernels (two copy
+ * streams owned by the library, three device slots in `work`).  Frames are
+ * planar and unpadded: frame f, plane c starts at element
+ * (f * n_planes + c) * height * width of host_in; host_out likewise at the
+ * output size pz_query reports.  Page-locked host memory is needed for the
+ * copies to overlap.  Asynchronous: `cuda_stream` completes once the last
+ * frame is in host_out.  work: device memory of pz_run_host_work_bytes()
+ * bytes, 256-byte aligned, not used by anything else until the stream has
+ * passed this call.  The copies first wait for the work already queued on
+ * cuda_stream (which may still use `work`); with PZ_HOST_WORK_IDLE in flags
+ * the caller vouches that `work` is idle, and the first frame's copy starts
+ * at once, so calls for several models overlap.  Replaces a host's
+ * per-frame upload, hook passes and readback. */
+#define PZ_HOST_WORK_IDLE 1
+size_t pz_run_host_work_bytes(const pz_model* model, int width, int height, int dtype, const pz_opts* opts);
+int pz_run_host(const pz_model* model, const void* host_in, void* host_out, int n_frames, int width, int height,
+                int dtype, const pz_opts* opts, void* work, size_t work_bytes, int flags, void* cuda_stream);
+
 /* ---- batched persistent execution ------------------------------------- */
 
 typedef struct {

@@ -25,6 +25,7 @@ PZ_LUMA, PZ_YUV, PZ_RGB = 0, 1, 2
 PZ_F32, PZ_F16 = 0, 1
 PZ_PREC_FP32, PZ_PREC_FAST, PZ_PREC_MPV = 0, 1, 2
 PZ_FILTER_BILINEAR, PZ_FILTER_CATMULL_ROM = 0, 1
+PZ_HOST_WORK_IDLE = 1
 
 
 class PrescaleLibraryError(RuntimeError):
@@ -93,6 +94,11 @@ EXPORTS = {
                                     ctypes.c_void_p]),
     "pz_nnedi3_run_static": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Plane), ctypes.POINTER(Plane),
                                             ctypes.POINTER(Opts), ctypes.c_void_p]),
+    "pz_run_host_work_bytes": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.POINTER(Opts)]),
+    "pz_run_host": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_int, ctypes.c_int, ctypes.POINTER(Opts), ctypes.c_void_p,
+                                   ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p]),
     "pz_resample": (ctypes.c_int, [ctypes.POINTER(Plane), ctypes.POINTER(Plane), ctypes.c_float, ctypes.c_float,
                                    ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_void_p]),
 }

@@ -304,18 +304,15 @@ class HookModel:
         return self._pack(res, planes, as_list, keys, return_keys)
 
     def upscale_host(self, frames, out=None, out_size: Optional[Tuple[int, int]] = None, precision: str = "fp32",
-                     device=None, depth: int = 3, wait: bool = True):
+                     device=None, wait: bool = True, stream=None):
         """Upscale host frames ``[N][C][H][W]`` (pinned CPU tensor) into host
-        memory, overlapping the copies with the kernels.
-
-        Frame i is copied to the device on a copy stream, upscaled on a
-        compute stream and copied back on a third stream, so the transfers
-        of neighbouring frames run under frame i's kernels.  ``depth`` device
-        buffers rotate (3: one in flight on each stream).  Returns the host
-        output ``[N][C][OH][OW]`` (``out`` if given; it should be pinned).
-        With ``wait=False`` it returns ``(out, event)`` as soon as the work is
-        queued: ``out`` is complete once ``event`` (a CUDA event) has
-        completed, so calls for several models can overlap on the device.
+        memory through ``pz_run_host``: frame i is copied in, run and copied
+        back while its neighbours' transfers run under its kernels.
+        Returns the host output ``[N][C][OH][OW]`` (``out`` if given; it
+        should be pinned).  With ``wait=False`` it returns ``(out, event)``
+        as soon as the work is queued: ``out`` is complete once ``event`` (a
+        CUDA event on ``stream``) has completed, so calls for several models
+        can overlap on the device.
         """
         torch = _torch()
         if frames.dim() != 4 or frames.is_cuda:
@@ -324,83 +321,44 @@ class HookModel:
             raise ValueError(f"{self.name} takes {self.n_planes} plane(s), got {frames.shape[1]}")
         if frames.dtype not in (torch.float32, torch.float16):
             raise ValueError("frames must be float32 or float16")
+        if not frames.is_contiguous():
+            raise ValueError("frames must be contiguous (the copies read them in place)")
         dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         N, C, H, W = frames.shape
+        if H == 0 or W == 0:
+            raise ValueError(f"empty frames {W}x{H}")
         if not self.enabled(W, H, out_size):   # //!WHEN false: the planes pass through
             out = frames.clone() if out is None else out.copy_(frames)
             return out if wait else (out, None)
         OW, OH = self.output_size(W, H, out_size)
         if out is None:
             out = torch.empty((N, C, OH, OW), dtype=frames.dtype, pin_memory=True)
-        with torch.cuda.device(dev):
-            s_in, s_run, s_out = torch.cuda.Stream(dev), torch.cuda.Stream(dev), torch.cuda.Stream(dev)
-            xin = [torch.empty((C, H, W), dtype=frames.dtype, device=dev) for _ in range(depth)]
-            yout = [torch.empty((C, OH, OW), dtype=frames.dtype, device=dev) for _ in range(depth)]
-            scratch = [None] * depth
-            if self.family == "nnedi3" and self.nnedi3_axes(W, H, out_size) == 3:
-                scratch = [torch.empty(2 * H * W * frames.element_size(), dtype=torch.uint8, device=dev)
-                           for _ in range(depth)]
-            # the pz_run arguments of each buffer, built once
-            calls = [self._prepared_call(list(xin[b].unbind(0)), list(yout[b].unbind(0)), (OW, OH), precision,
-                                         scratch[b]) for b in range(depth)]
-            copied = [torch.cuda.Event() for _ in range(depth)]
-            done = [torch.cuda.Event() for _ in range(depth)]
-            drained = [None] * depth
-            for i in range(N):
-                b = i % depth
-                if drained[b] is not None:       # buffer b's previous frame has left
-                    s_in.wait_event(drained[b])
-                with torch.cuda.stream(s_in):
-                    xin[b].copy_(frames[i], non_blocking=True)
-                    copied[b].record(s_in)
-                s_run.wait_event(copied[b])
-                if drained[b] is not None:
-                    s_run.wait_event(drained[b])
-                calls[b](s_run.cuda_stream)
-                done[b].record(s_run)
-                s_out.wait_event(done[b])
-                with torch.cuda.stream(s_out):
-                    out[i].copy_(yout[b], non_blocking=True)
-                    ev = torch.cuda.Event()
-                    ev.record(s_out)
-                    drained[b] = ev
-            for t in xin + yout + [x for x in scratch if x is not None]:   # used on side streams
-                t.record_stream(s_out)
-            if wait:
-                s_out.synchronize()
-                return out
-            fin = torch.cuda.Event()
-            fin.record(s_out)
-            return out, fin
-
-    def _prepared_call(self, pl, res, out_size, precision, scratch=None, staging="tma"):
-        """``pz_run`` on fixed tensors as a callable of the stream handle
-        (the ctypes arguments are built once)."""
-        torch = _torch()
-        dt = _ffi.PZ_F32 if pl[0].dtype == torch.float32 else _ffi.PZ_F16
-        n = len(pl)
-        pin = (_ffi.Plane * n)()
-        pout = (_ffi.Plane * n)()
-        for i, (p, r) in enumerate(zip(pl, res)):
-            pin[i] = _ffi.Plane(p.data_ptr(), p.shape[1], p.shape[0], p.stride(0), dt)
-            pout[i] = _ffi.Plane(r.data_ptr(), r.shape[1], r.shape[0], r.stride(0), dt)
+        elif tuple(out.shape) != (N, C, OH, OW) or out.dtype != frames.dtype or not out.is_contiguous():
+            raise ValueError(f"out must be a contiguous {frames.dtype} tensor of shape {(N, C, OH, OW)}")
+        dt = _ffi.PZ_F32 if frames.dtype == torch.float32 else _ffi.PZ_F16
         o = _ffi.Opts()
         o.precision = PRECISIONS[precision]
-        o.out_width, o.out_height = out_size
+        o.out_width, o.out_height = OW, OH
         if self.family == "nnedi3":
-            o.nnedi3_axes = self.nnedi3_axes(pl[0].shape[1], pl[0].shape[0], out_size)
-        if scratch is not None:
-            o.scratch = scratch.data_ptr()
-            o.scratch_bytes = scratch.numel() * scratch.element_size()
-        o.staging = STAGINGS[staging]
-        h = self.device_handle(pl[0].device.index)
+            o.nnedi3_axes = self.nnedi3_axes(W, H, out_size)
+        o.staging = STAGINGS["tma"]
         L = _ffi.lib()
-        po = _ffi.ctypes.byref(o)
-
-        def call(stream_handle):
-            _ffi.check(L.pz_run(h, pin, n, pout, n, po, stream_handle))
-        call.keep = (pl, res, scratch, pin, pout, o)   # the arguments live as long as the callable
-        return call
+        h = self.device_handle(dev.index)
+        with torch.cuda.device(dev):
+            s = stream if stream is not None else torch.cuda.current_stream(dev)
+            nbytes = L.pz_run_host_work_bytes(h, W, H, dt, _ffi.ctypes.byref(o))
+            # a fresh block of the caching allocator: idle, and kept from reuse
+            # until the stream has passed this call (record_stream below)
+            work = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=dev)
+            _ffi.check(L.pz_run_host(h, frames.data_ptr(), out.data_ptr(), N, W, H, dt, _ffi.ctypes.byref(o),
+                                     work.data_ptr(), work.numel(), _ffi.PZ_HOST_WORK_IDLE, s.cuda_stream))
+            work.record_stream(s)
+            if wait:
+                s.synchronize()
+                return out
+            fin = torch.cuda.Event()
+            fin.record(s)
+            return out, fin
 
     def key_shape(self, W, H, OW, OH):
         fam = self.family

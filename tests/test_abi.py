@@ -75,3 +75,9 @@ def test_query_arguments_are_checked_on_the_host(lib):
     r = _ffi.QueryResult()
     assert lib.pz_query(None, 8, 8, _ffi.PZ_F16, None, ctypes.byref(r)) == _ffi.PZ_EINVAL
     assert b"null" in lib.pz_last_error()
+
+
+def test_host_pipeline_arguments_are_checked_on_the_host(lib):
+    assert lib.pz_run_host(None, None, None, 1, 8, 8, _ffi.PZ_F16, None, None, 0, 0, None) == _ffi.PZ_EINVAL
+    assert b"null" in lib.pz_last_error()
+    assert lib.pz_run_host_work_bytes(None, 8, 8, _ffi.PZ_F16, None) == 0

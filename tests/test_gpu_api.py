@@ -44,6 +44,31 @@ def test_host_pipelines_of_two_models_overlap_and_match():
         assert torch.equal(yb[i], b.upscale(frames[i].cuda(), precision="fast").cpu())
 
 
+def test_host_pipeline_c_abi_checks_work_and_layout():
+    import ctypes
+    from mpv_prescalers_gb300 import _ffi, PrescaleError
+    hm, _ = synth.model_for("ravu-r3-yuv")
+    frames = torch.from_numpy(synth.yuv_frame(20, 28, 5))[None].to(torch.float16).pin_memory()
+    out = torch.empty((1, 3, 40, 56), dtype=torch.float16).pin_memory()
+    o = _ffi.Opts()
+    o.out_width, o.out_height = 56, 40
+    L = _ffi.lib()
+    h = hm.device_handle(0)
+    need = L.pz_run_host_work_bytes(h, 28, 20, _ffi.PZ_F16, ctypes.byref(o))
+    assert need >= 3 * (3 * 20 * 28 * 2 + 3 * 40 * 56 * 2)
+    work = torch.empty(need, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream()
+    rc = L.pz_run_host(h, frames.data_ptr(), out.data_ptr(), 1, 28, 20, _ffi.PZ_F16, ctypes.byref(o),
+                       work.data_ptr(), need - 256, 0, s.cuda_stream)
+    assert rc == _ffi.PZ_EINVAL and b"work" in L.pz_last_error()
+    _ffi.check(L.pz_run_host(h, frames.data_ptr(), out.data_ptr(), 1, 28, 20, _ffi.PZ_F16, ctypes.byref(o),
+                             work.data_ptr(), need, 0, s.cuda_stream))
+    s.synchronize()
+    assert torch.equal(out[0], hm.upscale(frames[0].cuda()).cpu())
+    with pytest.raises(ValueError, match="contiguous"):
+        hm.upscale_host(frames.transpose(2, 3))
+
+
 def test_host_pipeline_when_false_passes_frames_through():
     hm, _ = synth.model_for("ravu-lite-r3")
     frames = torch.rand((2, 1, 20, 30)).pin_memory()
