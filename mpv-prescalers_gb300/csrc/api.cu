@@ -276,15 +276,16 @@ int pz_model_create(const pz_model_desc* d, pz_model** out) {
     for (size_t i = 0; i < nval; i++) r[i] = __half2float(__float2half_rn(src[i]));
     return r;
   };
-  auto halves = [&](const float* src) {  // FP16 texels of the fast form
-    std::vector<__half> r(nval);
-    for (size_t i = 0; i < nval; i++) r[i] = __float2half_rn(src[i]);
-    return r;
-  };
+  // FP16 texels of the fast form, each row padded to an even texel count so
+  // that texel pairs are 16-byte loads
+  m->lut_h_pitch = (d->lut_cols + 1) & ~1;
+  std::vector<__half> luth((size_t)d->lut_rows * m->lut_h_pitch * 4, __float2half_rn(0.0f));
+  for (int r = 0; r < d->lut_rows; r++)
+    for (int c = 0; c < d->lut_cols * 4; c++)
+      luth[(size_t)r * m->lut_h_pitch * 4 + c] = __float2half_rn(d->lut[(size_t)r * d->lut_cols * 4 + c]);
   const std::vector<float> lut16 = rounded(d->lut);
-  const std::vector<__half> luth = halves(d->lut);
   if ((rc = upload(&m->d_lut, d->lut, bytes)) || (rc = upload(&m->d_lut16, lut16.data(), bytes)) ||
-      (rc = upload(&m->d_lut_h, luth.data(), nval * 2))) {
+      (rc = upload(&m->d_lut_h, luth.data(), luth.size() * 2))) {
     pz_model_destroy(m);
     return rc;
   }

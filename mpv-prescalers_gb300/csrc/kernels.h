@@ -27,6 +27,7 @@ struct RavuArgs {
   int staging;       // 0: clamped loads, 1: TMA boxes for interior tiles
   float lut_frac;    // zoom LUT bilinear fraction steps (0: exact FP32)
   const uint2* lut_h;  // fast form: the LUT as FP16 texels (4 halves each), or null
+  int lut_h_pitch;     // texels per FP16 LUT row (lut_cols rounded up to even)
   KeyParams kp;
 };
 

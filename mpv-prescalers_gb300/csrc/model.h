@@ -13,7 +13,8 @@ struct pz_model {
   float4* d_lut_ar = nullptr;
   float4* d_lut16 = nullptr;     // the LUTs with every value rounded to FP16
   float4* d_lut_ar16 = nullptr;
-  __half* d_lut_h = nullptr;     // the LUT as FP16 texels (fast form)
+  __half* d_lut_h = nullptr;     // the LUT as FP16 texels (fast form), rows padded
+  int lut_h_pitch = 0;           // to an even texel count (16-byte texel pairs)
   int lut_rows = 0, lut_cols = 0;
   pz::KeyParams kp{};
   int nns = 0, win_w = 0, win_h = 0;
@@ -50,5 +51,6 @@ inline void select_lut(const pz_model* m, int precision, RavuArgs* a) {
   a->lut_frac = mpv ? 256.0f : 0.0f;
   const bool h = fast_half_lut(m, precision);
   a->lut_h = h ? reinterpret_cast<const uint2*>(m->d_lut_h) : nullptr;
+  a->lut_h_pitch = m->lut_h_pitch;
 }
 }  // namespace pz

@@ -141,6 +141,17 @@ __device__ __forceinline__ float4 lut_texel(const float4* f, const uint2* h, siz
   }
 }
 
+// Two adjacent FP16 texels i, i+1 (i even) as one 16-byte load.
+__device__ __forceinline__ void lut_pair_h16(const uint2* h, size_t i, float4& a, float4& b) {
+  const uint4 q = __ldg(reinterpret_cast<const uint4*>(h + i));
+  const float2 a01 = __half22float2(*reinterpret_cast<const __half2*>(&q.x));
+  const float2 a23 = __half22float2(*reinterpret_cast<const __half2*>(&q.y));
+  const float2 b01 = __half22float2(*reinterpret_cast<const __half2*>(&q.z));
+  const float2 b23 = __half22float2(*reinterpret_cast<const __half2*>(&q.w));
+  a = make_float4(a01.x, a01.y, a23.x, a23.y);
+  b = make_float4(b01.x, b01.y, b23.x, b23.y);
+}
+
 // ------------------------------------------------------------ ravu-lite ---
 // Does lite LUT column c take part in the anti-ringing sums?  r2: every
 // tap; r3/r4: the 13-tap diamond |dx|+|dy| <= 2 (ravu-lite-ar-r3.hook:93-170).
@@ -174,7 +185,9 @@ struct LiteTile {
     structure_tensor<N, false>(get, p.kp, a, b, d);
     const int key = ravu_key(a, b, d, p.kp);
     if (p.keys) p.keys[(size_t)gy * p.W + gx] = key;
-    const size_t row = (size_t)min(max(key, 0), p.lut_rows - 1) * p.lut_cols;
+    const size_t row = (size_t)min(max(key, 0), p.lut_rows - 1) * (H16 ? p.lut_h_pitch : p.lut_cols);
+    float4 w_next;  // H16: the odd texel of the pair loaded at the even one
+    static_assert(S / 2 % 2 == 0, "texel pairs start at even columns");
     // FP32x2 sums: P = sum va*w, Q = sum vb*w, res = P + Q.wzyx; the
     // anti-ringing sums of output k as (hi, lo) and (hi2, lo2) pairs
     float2 P01 = make_float2(0.f, 0.f), P23 = P01, Q01 = P01, Q23 = P01;
@@ -183,7 +196,13 @@ struct LiteTile {
     for (int k = 0; k < 4; k++) HL[k] = HL3[k] = P01;
 #pragma unroll
     for (int c = 0; c < S / 2; c++) {
-      const float4 w = lut_texel<H16>(p.lut, p.lut_h, row + c);
+      float4 w;
+      if constexpr (H16) {
+        if (c % 2 == 0) lut_pair_h16(p.lut_h, row + c, w, w_next);
+        else w = w_next;
+      } else {
+        w = __ldg(p.lut + row + c);
+      }
       const float va = get(c / N, c % N), vb = get((S - 1 - c) / N, (S - 1 - c) % N);
       const float2 w01 = make_float2(w.x, w.y), w23 = make_float2(w.z, w.w);
       const float2 a2 = make_float2(va, va), b2 = make_float2(vb, vb);
@@ -207,8 +226,10 @@ struct LiteTile {
       }
     }
     {
-      constexpr int c = S / 2;
-      const float4 w = lut_texel<H16>(p.lut, p.lut_h, row + c);
+      constexpr int c = S / 2;  // even: the centre texel and the row's padding
+      float4 w;
+      if constexpr (H16) lut_pair_h16(p.lut_h, row + c, w, w_next);
+      else w = __ldg(p.lut + row + c);
       const float v = get(c / N, c % N);
       const float2 v2 = make_float2(v, v);
       P01 = __ffma2_rn(v2, make_float2(w.x, w.y), P01);
@@ -274,7 +295,7 @@ struct ThreeXTile {
     structure_tensor<N, false>(lum, p.kp, a, b, d);
     const int key = ravu_key(a, b, d, p.kp);
     if (p.keys) p.keys[(size_t)gy * p.W + gx] = key;
-    const size_t row = (size_t)min(max(key, 0), p.lut_rows - 1) * p.lut_cols;
+    const size_t row = (size_t)min(max(key, 0), p.lut_rows - 1) * (H16 ? p.lut_h_pitch : p.lut_cols);
     // res0 += a*w0 + b*w1.wzyx; res1 += a*w1 + b*w0.wzyx, as FP32x2 sums
     // P0 = sum a*w0, P1 = sum a*w1, Q0 = sum b*w0, Q1 = sum b*w1 (pairs .xy, .zw)
     float2 P0[C][2], P1[C][2], Q0[C][2], Q1[C][2];
@@ -284,8 +305,13 @@ struct ThreeXTile {
       for (int h = 0; h < 2; h++) P0[c][h] = P1[c][h] = Q0[c][h] = Q1[c][h] = make_float2(0.f, 0.f);
 #pragma unroll
     for (int t = 0; t < S / 2; t++) {
-      const float4 w0 = lut_texel<H16>(p.lut, p.lut_h, row + 2 * t);
-      const float4 w1 = lut_texel<H16>(p.lut, p.lut_h, row + 2 * t + 1);
+      float4 w0, w1;
+      if constexpr (H16) {
+        lut_pair_h16(p.lut_h, row + 2 * t, w0, w1);
+      } else {
+        w0 = __ldg(p.lut + row + 2 * t);
+        w1 = __ldg(p.lut + row + 2 * t + 1);
+      }
       const float2 w0a = make_float2(w0.x, w0.y), w0b = make_float2(w0.z, w0.w);
       const float2 w1a = make_float2(w1.x, w1.y), w1b = make_float2(w1.z, w1.w);
 #pragma unroll
@@ -303,8 +329,13 @@ struct ThreeXTile {
       }
     }
     constexpr int tc = S / 2;
-    const float4 w0 = lut_texel<H16>(p.lut, p.lut_h, row + 2 * tc);
-    const float4 w1 = lut_texel<H16>(p.lut, p.lut_h, row + 2 * tc + 1);
+    float4 w0, w1;
+    if constexpr (H16) {
+      lut_pair_h16(p.lut_h, row + 2 * tc, w0, w1);
+    } else {
+      w0 = __ldg(p.lut + row + 2 * tc);
+      w1 = __ldg(p.lut + row + 2 * tc + 1);
+    }
     float4 r0[C], r1[C];
 #pragma unroll
     for (int c = 0; c < C; c++) {
@@ -526,8 +557,9 @@ __device__ __forceinline__ ZoomPos zoom_pos(int X, int W, int OW) {
 // With q > 0 the fractions are rounded to multiples of 1/q, as a texture
 // unit's fixed-point filter weights are (q = 256: 8 fractional bits).
 template <bool H16>
-__device__ __forceinline__ float4 lut_bilinear(const float4* lut, const uint2* luth, int rows, int cols, int key,
-                                               int blk, float sx, float sy, float q) {
+__device__ __forceinline__ float4 lut_bilinear(const float4* lut, const uint2* luth, int hpitch, int rows, int cols,
+                                               int key, int blk, float sx, float sy, float q) {
+  const int pitch = H16 ? hpitch : cols;  // texels per stored row
   const float fx8 = 8.0f * sx, fy8 = 8.0f * sy;
   const float x0f = floorf(fx8), y0f = floorf(fy8);
   float fx = fx8 - x0f, fy = fy8 - y0f;
@@ -537,10 +569,10 @@ __device__ __forceinline__ float4 lut_bilinear(const float4* lut, const uint2* l
   }
   const int xa = min(blk * 9 + (int)x0f, cols - 1), xb = min(xa + 1, cols - 1);
   const int ya = clampi(key * 9 + (int)y0f, 0, rows - 1), yb = min(ya + 1, rows - 1);
-  const float4 v00 = lut_texel<H16>(lut, luth, (size_t)ya * cols + xa);
-  const float4 v01 = lut_texel<H16>(lut, luth, (size_t)ya * cols + xb);
-  const float4 v10 = lut_texel<H16>(lut, luth, (size_t)yb * cols + xa);
-  const float4 v11 = lut_texel<H16>(lut, luth, (size_t)yb * cols + xb);
+  const float4 v00 = lut_texel<H16>(lut, luth, (size_t)ya * pitch + xa);
+  const float4 v01 = lut_texel<H16>(lut, luth, (size_t)ya * pitch + xb);
+  const float4 v10 = lut_texel<H16>(lut, luth, (size_t)yb * pitch + xa);
+  const float4 v11 = lut_texel<H16>(lut, luth, (size_t)yb * pitch + xb);
   const float gx = 1.0f - fx, gy = 1.0f - fy;
   float4 r;
   r.x = (v00.x * gx + v01.x * fx) * gy + (v10.x * gx + v11.x * fx) * fy;
@@ -613,13 +645,13 @@ struct ZoomTile {
     }
 #pragma unroll
     for (int blk = 0; blk < NB; blk++) {
-      const float4 ws = lut_bilinear<H16>(p.lut, p.lut_h, p.lut_rows, p.lut_cols, key, blk, sx, sy, p.lut_frac);
-      const float4 wi = lut_bilinear<H16>(p.lut, p.lut_h, p.lut_rows, p.lut_cols, key, blk, ix, iy, p.lut_frac);
+      const float4 ws = lut_bilinear<H16>(p.lut, p.lut_h, p.lut_h_pitch, p.lut_rows, p.lut_cols, key, blk, sx, sy, p.lut_frac);
+      const float4 wi = lut_bilinear<H16>(p.lut, p.lut_h, p.lut_h_pitch, p.lut_rows, p.lut_cols, key, blk, ix, iy, p.lut_frac);
       float4 as = make_float4(0.f, 0.f, 0.f, 0.f), ai = as;
       if (AR) {  // the anti-ringing LUT stays FP32 in every form but mpv's (most of
                  // its values lie below FP16's normal range)
-        as = lut_bilinear<false>(p.lut_ar, nullptr, p.lut_rows, p.lut_cols, key, blk, sx, sy, p.lut_frac);
-        ai = lut_bilinear<false>(p.lut_ar, nullptr, p.lut_rows, p.lut_cols, key, blk, ix, iy, p.lut_frac);
+        as = lut_bilinear<false>(p.lut_ar, nullptr, 0, p.lut_rows, p.lut_cols, key, blk, sx, sy, p.lut_frac);
+        ai = lut_bilinear<false>(p.lut_ar, nullptr, 0, p.lut_rows, p.lut_cols, key, blk, ix, iy, p.lut_frac);
       }
 #pragma unroll
       for (int j = 0; j < 4; j++) {
