@@ -229,7 +229,10 @@ int pz_model_create(const pz_model_desc* d, pz_model** out) {
     return fail(PZ_EINVAL, "%d gradient weights, window needs %d", d->n_grad, pts);
   }
   pz::KeyParams& kp = m->kp;
-  for (int i = 0; i < d->n_grad; i++) kp.gw[i] = (float)d->grad_weights[i];
+  for (int i = 0; i < d->n_grad; i++) {
+    kp.gw[i] = (float)d->grad_weights[i];
+    kp.gwq[i] = kp.gw[i] * 0.25f;  // exact: a power-of-two scale
+  }
   kp.log2_mode = d->strength_log2;
   if (kp.log2_mode) {
     kp.log2_scale = d->strength_scale;

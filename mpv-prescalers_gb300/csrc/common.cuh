@@ -18,6 +18,7 @@ constexpr float kPi = 3.141592653589793f;    // the shaders' pi literal
 // Key quantisation constants of one model (kernel parameter).
 struct KeyParams {
   float gw[36];      // Gaussian weights of the gradient points (geometry order)
+  float gwq[36];     // gw / 4: the weights of two unhalved central differences
   float thr[3];      // strength thresholds (lite, zoom: 3; 3x: 2)
   int n_thr;
   int log2_mode;     // ravu: strength = clamp(floor(log2(l*scale+eps)), 0, max)
@@ -66,12 +67,17 @@ __device__ __forceinline__ float deriv(const G& s, int p) {
 
 // Gaussian-weighted sum of (gx^2, gx gy, gy^2) over the gradient points:
 // the whole window when N <= 4, else the window minus a one-tap border.
-// `get(kx, ky)` returns the key input at window grid (kx, ky).
-template <int N, bool FOUR, class Get>
+// `get(kx, ky)` returns the key input at window grid (kx, ky).  PACKED: a
+// and d accumulate as one FP32x2 pair, a += gx (gx w), d += gy (gy w),
+// b += (gx w) gy (three instructions per point instead of six; each term
+// rounds once more or less than the shader's gx * gx * w, far inside the
+// key's FP32 boundary budget).
+template <int N, bool FOUR, bool PACKED = true, class Get>
 __device__ __forceinline__ void structure_tensor(const Get& get, const KeyParams& kp, float& a,
                                                  float& b, float& d) {
   constexpr int P0 = N <= 4 ? 0 : 1;
   constexpr int P1 = N <= 4 ? N : N - 1;
+  float2 ad = make_float2(0.0f, 0.0f);
   a = 0.0f;
   b = 0.0f;
   d = 0.0f;
@@ -80,13 +86,31 @@ __device__ __forceinline__ void structure_tensor(const Get& get, const KeyParams
   for (int px = P0; px < P1; px++) {
 #pragma unroll
     for (int py = P0; py < P1; py++) {
-      float gx = deriv<N, FOUR>([&](int q) { return get(q, py); }, px);
-      float gy = deriv<N, FOUR>([&](int q) { return get(px, q); }, py);
-      float w = kp.gw[i++];
-      a += gx * gx * w;
-      b += gx * gy * w;
-      d += gy * gy * w;
+      // interior points of a window without the four-tap stencil (N > 4) are
+      // central differences; packed, their halving moves into the weight
+      // (gwq = gw / 4), which leaves every product bit for bit unchanged
+      constexpr bool kHalf = PACKED && !FOUR && N > 4;
+      const float gx = kHalf ? get(px + 1, py) - get(px - 1, py)
+                             : deriv<N, FOUR>([&](int q) { return get(q, py); }, px);
+      const float gy = kHalf ? get(px, py + 1) - get(px, py - 1)
+                             : deriv<N, FOUR>([&](int q) { return get(px, q); }, py);
+      const float w = kHalf ? kp.gwq[i] : kp.gw[i];
+      i++;
+      if constexpr (PACKED) {
+        const float2 g2 = make_float2(gx, gy);
+        const float2 gw2 = __fmul2_rn(g2, make_float2(w, w));
+        ad = __ffma2_rn(g2, gw2, ad);
+        b = fmaf(gw2.x, gy, b);
+      } else {
+        a += gx * gx * w;
+        b += gx * gy * w;
+        d += gy * gy * w;
+      }
     }
+  }
+  if constexpr (PACKED) {
+    a = ad.x;
+    d = ad.y;
   }
 }
 

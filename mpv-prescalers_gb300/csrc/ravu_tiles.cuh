@@ -141,6 +141,13 @@ __device__ __forceinline__ float4 lut_texel(const float4* f, const uint2* h, siz
   }
 }
 
+// Two adjacent FP32 texels i, i+1 (i even, row pitch even) as one 32-byte load.
+__device__ __forceinline__ void lut_pair_f32(const float4* f, size_t i, float4& a, float4& b) {
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+      : "l"(f + i));
+}
+
 // Two adjacent FP16 texels i, i+1 (i even) as one 16-byte load.
 __device__ __forceinline__ void lut_pair_h16(const uint2* h, size_t i, float4& a, float4& b) {
   const uint4 q = __ldg(reinterpret_cast<const uint4*>(h + i));
@@ -171,6 +178,9 @@ struct LiteTile {
   // ravu-lite-ar-r4 fits 5 CTAs per SM at <= 48 registers (measured 2 %
   // faster); the other radii lose more to spills than they gain
   static constexpr int kMinBlocks = (R == 4 && AR) ? 5 : 0;
+  // ravu-lite-ar-r2 / -r3 measured 2-5 % slower with the packed structure
+  // tensor (register allocation of the anti-ringing sums)
+  static constexpr bool kPackedTensor = !(R <= 3 && AR);
   using Elem = T;
 
   __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, const TmaCtx* tma = nullptr) {
@@ -182,7 +192,7 @@ struct LiteTile {
     if (gx >= p.W || gy >= p.H) return;
     auto get = [&](int kx, int ky) { return tile[(ty + ky) * TW + tx + kx]; };
     float a, b, d;
-    structure_tensor<N, false>(get, p.kp, a, b, d);
+    structure_tensor<N, false, kPackedTensor>(get, p.kp, a, b, d);
     const int key = ravu_key(a, b, d, p.kp);
     if (p.keys) p.keys[(size_t)gy * p.W + gx] = key;
     const size_t row = (size_t)min(max(key, 0), p.lut_rows - 1) * (H16 ? p.lut_h_pitch : p.lut_cols);
@@ -295,6 +305,8 @@ struct ThreeXTile {
     structure_tensor<N, false>(lum, p.kp, a, b, d);
     const int key = ravu_key(a, b, d, p.kp);
     if (p.keys) p.keys[(size_t)gy * p.W + gx] = key;
+    // 3x rows hold 2 * ceil(S / 2) texels: even, so the FP32 texel pairs are
+    // 32-byte aligned without padding (1.2x over two 16-byte loads)
     const size_t row = (size_t)min(max(key, 0), p.lut_rows - 1) * (H16 ? p.lut_h_pitch : p.lut_cols);
     // res0 += a*w0 + b*w1.wzyx; res1 += a*w1 + b*w0.wzyx, as FP32x2 sums
     // P0 = sum a*w0, P1 = sum a*w1, Q0 = sum b*w0, Q1 = sum b*w1 (pairs .xy, .zw)
@@ -306,12 +318,8 @@ struct ThreeXTile {
 #pragma unroll
     for (int t = 0; t < S / 2; t++) {
       float4 w0, w1;
-      if constexpr (H16) {
-        lut_pair_h16(p.lut_h, row + 2 * t, w0, w1);
-      } else {
-        w0 = __ldg(p.lut + row + 2 * t);
-        w1 = __ldg(p.lut + row + 2 * t + 1);
-      }
+      if constexpr (H16) lut_pair_h16(p.lut_h, row + 2 * t, w0, w1);
+      else lut_pair_f32(p.lut, row + 2 * t, w0, w1);
       const float2 w0a = make_float2(w0.x, w0.y), w0b = make_float2(w0.z, w0.w);
       const float2 w1a = make_float2(w1.x, w1.y), w1b = make_float2(w1.z, w1.w);
 #pragma unroll
@@ -330,12 +338,8 @@ struct ThreeXTile {
     }
     constexpr int tc = S / 2;
     float4 w0, w1;
-    if constexpr (H16) {
-      lut_pair_h16(p.lut_h, row + 2 * tc, w0, w1);
-    } else {
-      w0 = __ldg(p.lut + row + 2 * tc);
-      w1 = __ldg(p.lut + row + 2 * tc + 1);
-    }
+    if constexpr (H16) lut_pair_h16(p.lut_h, row + 2 * tc, w0, w1);
+    else lut_pair_f32(p.lut, row + 2 * tc, w0, w1);
     float4 r0[C], r1[C];
 #pragma unroll
     for (int c = 0; c < C; c++) {
