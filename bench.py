@@ -429,8 +429,9 @@ def run_gpu(args):
                              "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
                      # dram__bytes_read.sum + dram__bytes_write.sum of this kernel on one 1080p
                      # frame (ncu, profiles/lite_tile_h16_ravu-lite-ar-r4_1080p_fp16.md): the FP16
-                     # input plane; the 16.6 MB output is still in L2 when the launch ends
-                     "traffic": 4221440, "traffic_unit": "bytes per launch",
+                     # input plane (4.15 MB) with its tile halos and the LUT; the 16.6 MB output is
+                     # still in L2 when the launch ends
+                     "traffic": 4997120, "traffic_unit": "bytes per launch",
                      "algorithmic_bytes": algo_bytes},
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clocks,

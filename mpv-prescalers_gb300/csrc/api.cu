@@ -229,9 +229,19 @@ int pz_model_create(const pz_model_desc* d, pz_model** out) {
     return fail(PZ_EINVAL, "%d gradient weights, window needs %d", d->n_grad, pts);
   }
   pz::KeyParams& kp = m->kp;
-  for (int i = 0; i < d->n_grad; i++) {
-    kp.gw[i] = (float)d->grad_weights[i];
-    kp.gwq[i] = kp.gw[i] * 0.25f;  // exact: a power-of-two scale
+  {
+    // gradient points in kernel order (px outer, py inner); the stencil
+    // kind of each axis as in pz::stencil_kind
+    const bool four = d->family == PZ_RAVU || d->family == PZ_RAVU_ZOOM;
+    const int p0 = n <= 4 ? 0 : 1, p1 = n <= 4 ? n : n - 1;
+    auto kind = [&](int p) { return (p == 0 || p == n - 1) ? 0 : ((four && p >= 2 && p <= n - 3) ? 2 : 1); };
+    const double scale2[3] = {1.0, 0.25, 1.0 / 144.0};
+    int i = 0;
+    for (int px = p0; px < p1; px++)
+      for (int py = p0; py < p1; py++, i++) {
+        kp.gw[i] = (float)d->grad_weights[i];
+        kp.gwf[i] = kind(px) == kind(py) ? (float)((double)kp.gw[i] * scale2[kind(px)]) : kp.gw[i];
+      }
   }
   kp.log2_mode = d->strength_log2;
   if (kp.log2_mode) {

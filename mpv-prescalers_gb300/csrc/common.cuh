@@ -18,7 +18,8 @@ constexpr float kPi = 3.141592653589793f;    // the shaders' pi literal
 // Key quantisation constants of one model (kernel parameter).
 struct KeyParams {
   float gw[36];      // Gaussian weights of the gradient points (geometry order)
-  float gwq[36];     // gw / 4: the weights of two unhalved central differences
+  float gwf[36];     // gw * c^2 where both stencils of a point have the same scale c
+                     // (1 one-sided, 1/2 central, 1/12 four-tap), else gw
   float thr[3];      // strength thresholds (lite, zoom: 3; 3x: 2)
   int n_thr;
   int log2_mode;     // ravu: strength = clamp(floor(log2(l*scale+eps)), 0, max)
@@ -56,6 +57,21 @@ __device__ __forceinline__ float gl_mod(float x, float y) { return x - y * floor
 // Gradient stencil at grid position p along one axis of an N-tap window:
 // one-sided at the border, central /2 inside, and (FOUR: ravu, ravu-zoom)
 // (-s[p+2] + 8 s[p+1] - 8 s[p-1] + s[p-2]) / 12 where both exist.
+// stencil_kind: 0 one-sided, 1 central, 2 four-tap.
+template <int N, bool FOUR>
+__host__ __device__ constexpr int stencil_kind(int p) {
+  return (p == 0 || p == N - 1) ? 0 : ((FOUR && p >= 2 && p <= N - 3) ? 2 : 1);
+}
+
+// The stencil without its scale (1, 1/2, 1/12).
+template <int N, bool FOUR, class G>
+__device__ __forceinline__ float deriv_unscaled(const G& s, int p) {
+  if (p == 0) return s(1) - s(0);
+  if (p == N - 1) return s(N - 1) - s(N - 2);
+  if (FOUR && p >= 2 && p <= N - 3) return -s(p + 2) + 8.0f * s(p + 1) - 8.0f * s(p - 1) + s(p - 2);
+  return s(p + 1) - s(p - 1);
+}
+
 template <int N, bool FOUR, class G>
 __device__ __forceinline__ float deriv(const G& s, int p) {
   if (p == 0) return s(1) - s(0);
@@ -69,9 +85,11 @@ __device__ __forceinline__ float deriv(const G& s, int p) {
 // the whole window when N <= 4, else the window minus a one-tap border.
 // `get(kx, ky)` returns the key input at window grid (kx, ky).  PACKED: a
 // and d accumulate as one FP32x2 pair, a += gx (gx w), d += gy (gy w),
-// b += (gx w) gy (three instructions per point instead of six; each term
-// rounds once more or less than the shader's gx * gx * w, far inside the
-// key's FP32 boundary budget).
+// b += (gx w) gy (three instructions per point instead of six), and where
+// both stencils of a point share one scale c the scale moves into the weight
+// (gwf = gw c^2: the unscaled differences are used).  Each term then rounds
+// a few times differently from the shader's gx * gx * w, far inside the
+// key's FP32 boundary budget.
 template <int N, bool FOUR, bool PACKED = true, class Get>
 __device__ __forceinline__ void structure_tensor(const Get& get, const KeyParams& kp, float& a,
                                                  float& b, float& d) {
@@ -86,15 +104,12 @@ __device__ __forceinline__ void structure_tensor(const Get& get, const KeyParams
   for (int px = P0; px < P1; px++) {
 #pragma unroll
     for (int py = P0; py < P1; py++) {
-      // interior points of a window without the four-tap stencil (N > 4) are
-      // central differences; packed, their halving moves into the weight
-      // (gwq = gw / 4), which leaves every product bit for bit unchanged
-      constexpr bool kHalf = PACKED && !FOUR && N > 4;
-      const float gx = kHalf ? get(px + 1, py) - get(px - 1, py)
-                             : deriv<N, FOUR>([&](int q) { return get(q, py); }, px);
-      const float gy = kHalf ? get(px, py + 1) - get(px, py - 1)
-                             : deriv<N, FOUR>([&](int q) { return get(px, q); }, py);
-      const float w = kHalf ? kp.gwq[i] : kp.gw[i];
+      const bool fold = PACKED && stencil_kind<N, FOUR>(px) == stencil_kind<N, FOUR>(py);
+      auto sx = [&](int q) { return get(q, py); };
+      auto sy = [&](int q) { return get(px, q); };
+      const float gx = fold ? deriv_unscaled<N, FOUR>(sx, px) : deriv<N, FOUR>(sx, px);
+      const float gy = fold ? deriv_unscaled<N, FOUR>(sy, py) : deriv<N, FOUR>(sy, py);
+      const float w = fold ? kp.gwf[i] : kp.gw[i];
       i++;
       if constexpr (PACKED) {
         const float2 g2 = make_float2(gx, gy);
@@ -196,10 +211,12 @@ __device__ __forceinline__ void ar_pow2(float v, float2& p32, float2& p33) {
   p33 = __fmul2_rn(q, hl);
 }
 
-// lo = 1.1 - lo2/lo; hi = hi2/hi - 0.1; mix(res, clamp(res, lo, hi), s)
+// lo = 1.1 - lo2/lo; hi = hi2/hi - 0.1; mix(res, clamp(res, lo, hi), s).
+// The quotients are approximate (__fdividef, about 2 ulp, the precision a
+// shader's division has): they only move the clamp bounds, by < 3e-7.
 __device__ __forceinline__ float ar_finish(float res, float lo, float hi, float lo2, float hi2, float s) {
-  float lob = 1.1f - lo2 / lo;
-  float hib = hi2 / hi - 0.1f;
+  float lob = 1.1f - __fdividef(lo2, lo);
+  float hib = __fdividef(hi2, hi) - 0.1f;
   float c = fminf(fmaxf(res, lob), hib);
   return res * (1.0f - s) + c * s;
 }

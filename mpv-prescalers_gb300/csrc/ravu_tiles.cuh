@@ -598,7 +598,10 @@ struct ZoomTile {
   static constexpr int RW = kTileW + N + 1, RH = kTileH + N + 1;
   static constexpr int C = CM == kLuma ? 1 : 3;
   static constexpr int NB = (S / 2 + 3) / 4;  // LUT texels per half window
-  static constexpr size_t smem_bytes = (size_t)(C + (CM == kRgb ? 1 : 0)) * RW * RH * 4;
+  // input rectangle planes, then the source positions of the tile's 32
+  // columns and 8 rows
+  static constexpr size_t smem_bytes =
+      (size_t)(C + (CM == kRgb ? 1 : 0)) * RW * RH * 4 + (kTileW + kTileH) * sizeof(ZoomPos);
 
   static constexpr int kPlanes = 0;  // the input rectangle moves with the ratio: clamped loads only
   static constexpr int kMinBlocks = 0;  // no launch-bounds minimum
@@ -607,9 +610,15 @@ struct ZoomTile {
   __device__ static void run(const RavuArgs& p, int X0, int Y0, float* smem, const TmaCtx* = nullptr) {
     float* tile = smem;
     float* ltile = smem + C * RW * RH;
+    ZoomPos* pos = reinterpret_cast<ZoomPos*>(smem + (C + (CM == kRgb ? 1 : 0)) * RW * RH);
     const int X1 = min(X0 + kTileW - 1, p.OW - 1), Y1 = min(Y0 + kTileH - 1, p.OH - 1);
-    const int rx = zoom_pos(X0, p.W, p.OW).i - LO, ry = zoom_pos(Y0, p.H, p.OH).i - LO;
-    const int rw = zoom_pos(X1, p.W, p.OW).i + R - rx + 1, rh = zoom_pos(Y1, p.H, p.OH).i + R - ry + 1;
+    if (threadIdx.x < kTileW + kTileH) {  // one exact position per tile column / row
+      const int t = threadIdx.x;
+      pos[t] = t < kTileW ? zoom_pos(min(X0 + t, X1), p.W, p.OW) : zoom_pos(min(Y0 + t - kTileW, Y1), p.H, p.OH);
+    }
+    __syncthreads();
+    const int rx = pos[0].i - LO, ry = pos[kTileW].i - LO;
+    const int rw = pos[X1 - X0].i + R - rx + 1, rh = pos[kTileW + Y1 - Y0].i + R - ry + 1;
     if (rw > RW || rh > RH) {  // only reachable when downscaling, which the host rejects
       if (threadIdx.x == 0 && p.err) atomicCAS(p.err, 0, kErrTileOverflow);
       return;
@@ -628,7 +637,7 @@ struct ZoomTile {
     __syncthreads();
     const int X = X0 + threadIdx.x % kTileW, Y = Y0 + threadIdx.x / kTileW;
     if (X >= p.OW || Y >= p.OH) return;
-    const ZoomPos px = zoom_pos(X, p.W, p.OW), py = zoom_pos(Y, p.H, p.OH);
+    const ZoomPos px = pos[threadIdx.x % kTileW], py = pos[kTileW + threadIdx.x / kTileW];
     const int bx = px.i - LO - rx, by = py.i - LO - ry;  // window origin in the tile
     auto val = [&](int c, int k) { return tile[c * RW * RH + (by + k % N) * RW + bx + k / N]; };
     auto lum = [&](int kx, int ky) {
