@@ -171,7 +171,8 @@ template <int R, bool AR, typename T, bool H16 = false>
 struct LiteTile {
   static constexpr int N = 2 * R - 1, S = N * N, HALO = R - 1;
   static constexpr int TW = kTileW + N - 1, TH = kTileH + N - 1;
-  // value tile, then (AR) the anti-ringing powers of every tile value
+  // the value tile; the anti-ringing powers are formed per tap in registers
+  // (ar_pow2)
   static constexpr size_t smem_bytes = (size_t)((TW * TH + 3) & ~3) * 4;
 
   static constexpr int kPlanes = 1;
@@ -417,9 +418,10 @@ struct Int11Tile {
   static constexpr int C = CM == kLuma ? 1 : 3;
   static constexpr size_t smem_bytes = (size_t)(C + (CM == kRgb ? 1 : 0)) * TW * TH * 4;
   static constexpr int kPlanes = C;
-  // register caps measured best on GB300: r3 8 CTAs per SM, r4 5, r2 the
+  // register caps measured best on GB300: r3 6 CTAs per SM (40 registers;
+  // 8 CTAs at 32 spill the packed structure tensor), r4 5, r2 the
   // compiler's own allocation
-  static constexpr int kMinBlocks = R == 3 ? 8 : (R == 4 ? 5 : 0);
+  static constexpr int kMinBlocks = R == 3 ? 6 : (R == 4 ? 5 : 0);
   using Elem = T;
 
   __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, const TmaCtx* tma = nullptr) {

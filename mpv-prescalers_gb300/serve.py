@@ -151,8 +151,10 @@ class Server:
         slot.reqs = reqs
 
     def run(self, trace: Sequence[Request], max_group: int = 4) -> Dict[str, float]:
-        """Serve a trace in real time; returns latency / throughput stats."""
+        """Serve a trace in real time; returns latency / throughput stats
+        (the HBM peak is this run's)."""
         torch = _torch()
+        self.peak = self.in_use
         pending = sorted(trace, key=lambda r: r.arrival)
         queue: List[Request] = []
         t0_event = torch.cuda.Event(enable_timing=True)
