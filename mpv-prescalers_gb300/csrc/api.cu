@@ -230,17 +230,17 @@ int pz_model_create(const pz_model_desc* d, pz_model** out) {
   }
   pz::KeyParams& kp = m->kp;
   {
-    // gradient points in kernel order (px outer, py inner); the stencil
-    // kind of each axis as in pz::stencil_kind
+    // gradient points in kernel order (px outer, py inner); where both
+    // stencils of a point share one scale c, gwf = gw c^2
     const bool four = d->family == PZ_RAVU || d->family == PZ_RAVU_ZOOM;
     const int p0 = n <= 4 ? 0 : 1, p1 = n <= 4 ? n : n - 1;
-    auto kind = [&](int p) { return (p == 0 || p == n - 1) ? 0 : ((four && p >= 2 && p <= n - 3) ? 2 : 1); };
-    const double scale2[3] = {1.0, 0.25, 1.0 / 144.0};
+    const double scale2[3] = {1.0, 0.25, 1.0 / 144.0};  // c^2 per stencil kind
     int i = 0;
     for (int px = p0; px < p1; px++)
       for (int py = p0; py < p1; py++, i++) {
+        const int kx = pz::stencil_kind(n, four, px), ky = pz::stencil_kind(n, four, py);
         kp.gw[i] = (float)d->grad_weights[i];
-        kp.gwf[i] = kind(px) == kind(py) ? (float)((double)kp.gw[i] * scale2[kind(px)]) : kp.gw[i];
+        kp.gwf[i] = kx == ky ? (float)((double)kp.gw[i] * scale2[kx]) : kp.gw[i];
       }
   }
   kp.log2_mode = d->strength_log2;

@@ -57,10 +57,10 @@ __device__ __forceinline__ float gl_mod(float x, float y) { return x - y * floor
 // Gradient stencil at grid position p along one axis of an N-tap window:
 // one-sided at the border, central /2 inside, and (FOUR: ravu, ravu-zoom)
 // (-s[p+2] + 8 s[p+1] - 8 s[p-1] + s[p-2]) / 12 where both exist.
-// stencil_kind: 0 one-sided, 1 central, 2 four-tap.
-template <int N, bool FOUR>
-__host__ __device__ constexpr int stencil_kind(int p) {
-  return (p == 0 || p == N - 1) ? 0 : ((FOUR && p >= 2 && p <= N - 3) ? 2 : 1);
+// stencil_kind: 0 one-sided, 1 central, 2 four-tap (also used on the host
+// to scale the weights of KeyParams::gwf).
+__host__ __device__ constexpr int stencil_kind(int n, bool four, int p) {
+  return (p == 0 || p == n - 1) ? 0 : ((four && p >= 2 && p <= n - 3) ? 2 : 1);
 }
 
 // The stencil without its scale (1, 1/2, 1/12).
@@ -104,7 +104,7 @@ __device__ __forceinline__ void structure_tensor(const Get& get, const KeyParams
   for (int px = P0; px < P1; px++) {
 #pragma unroll
     for (int py = P0; py < P1; py++) {
-      const bool fold = PACKED && stencil_kind<N, FOUR>(px) == stencil_kind<N, FOUR>(py);
+      const bool fold = PACKED && stencil_kind(N, FOUR, px) == stencil_kind(N, FOUR, py);
       auto sx = [&](int q) { return get(q, py); };
       auto sy = [&](int q) { return get(px, q); };
       const float gx = fold ? deriv_unscaled<N, FOUR>(sx, px) : deriv<N, FOUR>(sx, px);
