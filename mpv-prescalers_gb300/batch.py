@@ -23,7 +23,7 @@ from dataclasses import dataclass, field
 from typing import Dict, List, Optional, Sequence, Tuple
 
 from . import _ffi
-from .prescaler import PRECISIONS, HookModel
+from .prescaler import PRECISIONS, STAGINGS, HookModel
 
 
 def _torch():
@@ -40,9 +40,10 @@ class Job:
     out_size: Optional[Tuple[int, int]] = None
     precision: str = "fp32"
     scratch: Optional["torch.Tensor"] = None
+    staging: str = "tma"   # RAVU halo staging of interior tiles: "tma" boxes or "ldg" clamped loads
 
     @staticmethod
-    def make(model: HookModel, frame, out_size=None, precision="fp32", out=None) -> "Job":
+    def make(model: HookModel, frame, out_size=None, precision="fp32", out=None, staging="tma") -> "Job":
         """A job for ``frame`` ([H][W] or [C][H][W] CUDA tensor); allocates
         the outputs (and NNEDI3 scratch) unless ``out`` is given."""
         torch = _torch()
@@ -56,11 +57,13 @@ class Job:
         scratch = None
         if model.family == "nnedi3" and model.nnedi3_axes(W, H, (OW, OH)) == 3:
             scratch = torch.empty(2 * H * W * pl[0].element_size(), dtype=torch.uint8, device=pl[0].device)
-        return Job(model, pl, outs, (OW, OH), precision, scratch)
+        if staging not in STAGINGS:
+            raise ValueError(f"staging {staging!r}: one of {sorted(STAGINGS)}")
+        return Job(model, pl, outs, (OW, OH), precision, scratch, staging)
 
     def signature(self) -> Tuple:
         p = self.inputs[0]
-        return (self.model.name, p.shape[1], p.shape[0], self.out_size, str(p.dtype), self.precision)
+        return (self.model.name, p.shape[1], p.shape[0], self.out_size, str(p.dtype), self.precision, self.staging)
 
     def to_c(self) -> _ffi.Job:
         torch = _torch()
@@ -72,6 +75,7 @@ class Job:
             j.out[i] = _ffi.Plane(o.data_ptr(), o.shape[1], o.shape[0], o.stride(0), dt)
         j.n_planes = len(self.inputs)
         j.opts.precision = PRECISIONS[self.precision]
+        j.opts.staging = STAGINGS[self.staging]
         j.opts.out_width, j.opts.out_height = self.out_size
         if self.model.family == "nnedi3":
             W, H = self.inputs[0].shape[1], self.inputs[0].shape[0]

@@ -132,6 +132,11 @@ int build_tables(const pz_job* jobs, int n, std::vector<pz::DevJob>* table, pz_b
     const int th = ((zoom ? a.OH : a.H) + pz::kTileH - 1) / pz::kTileH;
     d.tiles_w = tw;
     d.first_tile = g.total_tiles;
+    // interior tiles of jobs that ask for TMA staging come in as TMA boxes
+    // (the maps live in the device table); a map the driver rejects leaves
+    // the job on clamped loads
+    a.staging = j.opts.staging;
+    d.has_maps = j.opts.staging == 1 && g.ops.encode && g.ops.encode(a, &d.maps) ? 1 : 0;
     g.total_tiles += tw * th;
     table->push_back(d);
     g.n_jobs++;

@@ -44,7 +44,7 @@ PersistentOps lattice_ops(int prog) {
     PZ_P(kLattice0 + 8, LatticeTile, 4, kRgb)
   }
 #undef PZ_P
-  return {nullptr, nullptr};
+  return {nullptr, nullptr, nullptr};
 }
 
 }  // namespace

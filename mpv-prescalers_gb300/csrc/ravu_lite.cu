@@ -56,7 +56,7 @@ PersistentOps lite_ops(int prog) {
   }
 #undef PZ_L
 #undef PZ_X
-  return {nullptr, nullptr};
+  return {nullptr, nullptr, nullptr};
 }
 
 }  // namespace

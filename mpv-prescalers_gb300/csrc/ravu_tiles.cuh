@@ -68,9 +68,11 @@ struct TmaMaps {
 };
 
 struct TmaCtx {
-  const CUtensorMap* map;  // one per plane, in kernel parameter space
-  uint32_t mbar;           // shared mbarrier (count 1), used once
+  const CUtensorMap* map;  // one per plane (kernel parameter or global memory); null: clamped loads
+  uint32_t mbar;           // shared mbarrier (count 1)
   unsigned char* raw;      // landing area, 128-byte aligned
+  uint32_t phase;          // parity of the mbarrier's next completion (flips per TMA-staged tile)
+  int dead;                // a wait timed out: this CTA stages by clamped loads from now on
 };
 
 template <int TW>
@@ -85,24 +87,29 @@ __host__ __device__ constexpr uint32_t tma_plane_bytes() {
 __device__ __forceinline__ float lds_f(const float* p) { return *p; }
 __device__ __forceinline__ float lds_f(const __half* p) { return __half2float(*p); }
 
-// 1: staged by TMA; 0: not an interior tile (use clamped loads); -1: the
-// copy did not complete within the wait bound (error word set).
+// 1: staged by TMA; 0: not an interior tile, or no maps (use clamped
+// loads); -1: the copy did not complete within the wait bound (error word
+// set, the tile abandoned and TMA off for the rest of the CTA).  The outcome
+// of the wait is made uniform across the CTA, so every thread takes the same
+// path through the tile's barriers.
 template <int CM, int TW, int TH, typename T>
-__device__ int stage_planes_tma(const RavuArgs& p, const TmaCtx* t, int x0, int y0, float* tile, float* ltile) {
+__device__ int stage_planes_tma(const RavuArgs& p, TmaCtx* t, int x0, int y0, float* tile, float* ltile) {
   constexpr int C = CM == kLuma ? 1 : 3;
   constexpr int BW = tma_box_w<TW>();
   constexpr uint32_t PB = tma_plane_bytes<TW, TH, T>();
-  if (!t || x0 < 0 || y0 < 0 || x0 + TW > p.W || y0 + TH > p.H) return 0;
+  if (!t || !t->map || t->dead || x0 < 0 || y0 < 0 || x0 + TW > p.W || y0 + TH > p.H) return 0;
   const int bx = x0 & ~7, off = x0 - bx;
   if (threadIdx.x == 0) {
     mbar_arrive_expect_tx(t->mbar, (uint32_t)C * BW * TH * sizeof(T));
 #pragma unroll
     for (int c = 0; c < C; c++) tma_load_2d(t->raw + c * PB, &t->map[c], bx, y0, t->mbar);
   }
-  if (!mbar_wait_bounded(t->mbar, 0)) {
+  if (!__syncthreads_and(mbar_wait_bounded(t->mbar, t->phase))) {
     if (threadIdx.x == 0 && p.err) atomicCAS(p.err, 0, kErrWaitTimeout);
+    t->dead = 1;
     return -1;
   }
+  t->phase ^= 1u;
   for (int i = threadIdx.x; i < TW * TH; i += kTileThreads) {
     const int ty = i / TW, tx = i % TW;
     float v[3] = {0.f, 0.f, 0.f};
@@ -119,7 +126,7 @@ __device__ int stage_planes_tma(const RavuArgs& p, const TmaCtx* t, int x0, int 
 // Stage the frame tile by TMA when possible, else by clamped loads.
 // Returns false only when a TMA wait timed out (the tile is abandoned).
 template <int CM, int TW, int TH, typename T>
-__device__ __forceinline__ bool stage_frame(const RavuArgs& p, const TmaCtx* t, int x0, int y0, float* tile,
+__device__ __forceinline__ bool stage_frame(const RavuArgs& p, TmaCtx* t, int x0, int y0, float* tile,
                                             float* ltile) {
   const int r = stage_planes_tma<CM, TW, TH, T>(p, t, x0, y0, tile, ltile);
   if (r == 0) stage_planes<CM, TW, TH, T>(tile, ltile, p, x0, y0);
@@ -184,7 +191,7 @@ struct LiteTile {
   static constexpr bool kPackedTensor = !(R <= 3 && AR);
   using Elem = T;
 
-  __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, const TmaCtx* tma = nullptr) {
+  __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, TmaCtx* tma = nullptr) {
     float* tile = smem;
     if (!stage_frame<kLuma, TW, TH, T>(p, tma, x0 - HALO, y0 - HALO, tile, nullptr)) return;
     __syncthreads();
@@ -290,7 +297,7 @@ struct ThreeXTile {
   static constexpr int kMinBlocks = 0;  // no launch-bounds minimum
   using Elem = T;
 
-  __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, const TmaCtx* tma = nullptr) {
+  __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, TmaCtx* tma = nullptr) {
     float* tile = smem;
     float* ltile = smem + C * TW * TH;
     if (!stage_frame<CM, TW, TH, T>(p, tma, x0 - HALO, y0 - HALO, tile, ltile)) return;
@@ -424,7 +431,7 @@ struct Int11Tile {
   static constexpr int kMinBlocks = R == 3 ? 6 : (R == 4 ? 5 : 0);
   using Elem = T;
 
-  __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, const TmaCtx* tma = nullptr) {
+  __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, TmaCtx* tma = nullptr) {
     float* tile = smem;
     float* ltile = smem + C * TW * TH;
     if (!stage_frame<CM, TW, TH, T>(p, tma, x0 - HALO, y0 - HALO, tile, ltile)) return;
@@ -490,7 +497,7 @@ struct LatticeTile {
   static constexpr int kMinBlocks = R == 3 ? 5 : (R == 4 ? 3 : 0);
   using Elem = T;
 
-  __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, const TmaCtx* tma = nullptr) {
+  __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, TmaCtx* tma = nullptr) {
     float* tin = smem;                      // input, offsets -(R-1) .. R
     float* lin = tin + C * TW * TH;
     float* t11 = smem + PL * TW * TH;       // int11, offsets -R .. R-1
@@ -609,7 +616,7 @@ struct ZoomTile {
   static constexpr int kMinBlocks = 0;  // no launch-bounds minimum
   using Elem = T;
 
-  __device__ static void run(const RavuArgs& p, int X0, int Y0, float* smem, const TmaCtx* = nullptr) {
+  __device__ static void run(const RavuArgs& p, int X0, int Y0, float* smem, TmaCtx* = nullptr) {
     float* tile = smem;
     float* ltile = smem + C * RW * RH;
     ZoomPos* pos = reinterpret_cast<ZoomPos*>(smem + (C + (CM == kRgb ? 1 : 0)) * RW * RH);
@@ -712,7 +719,7 @@ __device__ __forceinline__ void tile_body(const RavuArgs& p, const TmaMaps& maps
     if (threadIdx.x == 0) mbar_init(smem_u32(&mbar), 1);
     __syncthreads();
     TmaCtx ctx{maps.map, smem_u32(&mbar),
-               reinterpret_cast<unsigned char*>(tile_smem) + ((Prog::smem_bytes + 127) & ~(size_t)127)};
+               reinterpret_cast<unsigned char*>(tile_smem) + ((Prog::smem_bytes + 127) & ~(size_t)127), 0u, 0};
     Prog::run(p, blockIdx.x * kTileW, blockIdx.y * kTileH, smem, &ctx);
   } else {
     Prog::run(p, blockIdx.x * kTileW, blockIdx.y * kTileH, smem, nullptr);
@@ -782,13 +789,16 @@ enum ProgId : int {
   kNumProgs = 72
 };
 
-// One batch job: a frame's arguments and its place in its launch's tile range.
+// One batch job: a frame's arguments, its place in its launch's tile range
+// and (has_maps) the TMA maps of its input planes, read by the TMA unit
+// from global memory.
 struct DevJob {
   RavuArgs a;
   int prog;
   int tiles_w;
   int first_tile;  // prefix sum within its launch group
-  int pad;
+  int has_maps;
+  TmaMaps maps;    // 64-byte aligned (CUtensorMap)
 };
 
 // Persistent CTAs of one tile program: claim tile numbers from `counter`
@@ -802,6 +812,13 @@ __device__ __forceinline__ void persistent_body(const DevJob* __restrict__ jobs,
   extern __shared__ __align__(128) float4 psmem[];
   float* smem = reinterpret_cast<float*>(psmem);
   __shared__ RavuArgs s_args;
+  // TMA staging of interior tiles (jobs with maps; programs with planes):
+  // the landing area follows the program's shared memory; the mbarrier is
+  // initialised before the first claim barrier, which orders it before use
+  __shared__ __align__(8) unsigned long long mbar;
+  if (Prog::kPlanes > 0 && threadIdx.x == 0) mbar_init(smem_u32(&mbar), 1);
+  TmaCtx ctx{nullptr, smem_u32(&mbar),
+             reinterpret_cast<unsigned char*>(psmem) + ((Prog::smem_bytes + 127) & ~(size_t)127), 0u, 0};
   // claim slots alternate between iterations: thread 0 fills slot (i+1)&1
   // while the other threads may still read slot i&1, and cannot get two
   // iterations ahead (the claim barrier of iteration i+1 holds it)
@@ -836,13 +853,14 @@ __device__ __forceinline__ void persistent_body(const DevJob* __restrict__ jobs,
       const int* src = reinterpret_cast<const int*>(&jobs[loaded].a);
       int* dst = reinterpret_cast<int*>(&s_args);
       for (int i = threadIdx.x; i < (int)(sizeof(RavuArgs) / 4); i += kTileThreads) dst[i] = src[i];
+      ctx.map = jobs[loaded].has_maps ? jobs[loaded].maps.map : nullptr;
       __syncthreads();
     }
     const int t = item - first;
     // No barrier after the tile: the next tile's staging and argument copy
     // come after the next claim barrier, which every thread reaches only
     // when done with this tile.
-    Prog::run(s_args, (t % tw) * kTileW, (t / tw) * kTileH, smem, nullptr);
+    Prog::run(s_args, (t % tw) * kTileW, (t / tw) * kTileH, smem, Prog::kPlanes > 0 ? &ctx : nullptr);
   }
 }
 
@@ -857,35 +875,62 @@ __global__ void __launch_bounds__(kTileThreads, Prog::kMinBlocks) persistent_ker
   persistent_body<Prog>(jobs, n_jobs, total, counter);
 }
 
-// Launch and occupancy query of one program's persistent kernel.
+// Launch, occupancy query and TMA map encoding of one program's persistent
+// kernel.
 struct PersistentOps {
   void (*launch)(const DevJob* jobs, int n_jobs, int total, int* counter, int grid, cudaStream_t s);
-  int (*fit)();  // resident CTAs per SM
+  int (*fit)();                                     // resident CTAs per SM
+  bool (*encode)(const RavuArgs& a, TmaMaps* maps);  // false: the program stages by clamped loads
 };
+
+// Shared memory of a persistent CTA: the program's, then (programs with
+// planes) the TMA landing area of every plane.
+template <class Prog>
+constexpr size_t persistent_smem() {
+  if constexpr (Prog::kPlanes > 0)
+    return ((Prog::smem_bytes + 127) & ~(size_t)127) +
+           (size_t)Prog::kPlanes * tma_plane_bytes<Prog::TW, Prog::TH, typename Prog::Elem>();
+  else
+    return Prog::smem_bytes;
+}
+
+template <class Prog>
+bool persistent_encode(const RavuArgs& a, TmaMaps* maps) {
+  if constexpr (Prog::kPlanes > 0) {
+    constexpr int BW = tma_box_w<Prog::TW>(), BH = Prog::TH;
+    const int dt = sizeof(typename Prog::Elem) == 4 ? 0 : 1;
+    for (int c = 0; c < Prog::kPlanes; c++)
+      if (!encode_plane_map(&maps->map[c], a.in[c], a.W, a.H, a.in_pitch[c], dt, BW, BH)) return false;
+    return true;
+  } else {
+    return false;
+  }
+}
 
 template <class Prog>
 PersistentOps persistent_ops() {
-  static_assert(Prog::smem_bytes <= 48 * 1024, "tile program needs more than the default shared memory");
+  constexpr size_t kSmem = persistent_smem<Prog>();
+  static_assert(kSmem <= 48 * 1024, "persistent tile program needs more than the default shared memory");
   if constexpr (Prog::kMinBlocks > 0) {
     return {[](const DevJob* j, int n, int total, int* c, int grid, cudaStream_t s) {
-              persistent_kernel_mb<Prog><<<grid, kTileThreads, Prog::smem_bytes, s>>>(j, n, total, c);
+              persistent_kernel_mb<Prog><<<grid, kTileThreads, kSmem, s>>>(j, n, total, c);
             },
             []() {
               int fit = 0;
-              cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, persistent_kernel_mb<Prog>, kTileThreads,
-                                                            Prog::smem_bytes);
+              cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, persistent_kernel_mb<Prog>, kTileThreads, kSmem);
               return fit;
-            }};
+            },
+            persistent_encode<Prog>};
   } else {
     return {[](const DevJob* j, int n, int total, int* c, int grid, cudaStream_t s) {
-              persistent_kernel<Prog><<<grid, kTileThreads, Prog::smem_bytes, s>>>(j, n, total, c);
+              persistent_kernel<Prog><<<grid, kTileThreads, kSmem, s>>>(j, n, total, c);
             },
             []() {
               int fit = 0;
-              cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, persistent_kernel<Prog>, kTileThreads,
-                                                            Prog::smem_bytes);
+              cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, persistent_kernel<Prog>, kTileThreads, kSmem);
               return fit;
-            }};
+            },
+            persistent_encode<Prog>};
   }
 }
 

@@ -43,7 +43,7 @@ PersistentOps zoom_ops(int prog) {
     PZ_Z(kZoomH0 + 10, 3, kRgb, false, true) PZ_Z(kZoomH0 + 11, 3, kRgb, true, true)
   }
 #undef PZ_Z
-  return {nullptr, nullptr};
+  return {nullptr, nullptr, nullptr};
 }
 
 }  // namespace
