@@ -38,12 +38,12 @@ MIX = [  # (model, H, W, dtype, out_size, precision)
 ]
 
 
-def _jobs(seed=0):
+def _jobs(seed=0, staging="tma"):
     jobs = []
     for i, (name, H, W, dt, osz, prec) in enumerate(MIX):
         hm, _ = synth.model_for(name)
         x = torch.from_numpy(synth.frame(H, W, 300 + i + seed, hm.channels)).to("cuda", dt)
-        jobs.append(B.Job.make(hm, x, out_size=osz, precision=prec))
+        jobs.append(B.Job.make(hm, x, out_size=osz, precision=prec, staging=staging))
     return jobs
 
 
@@ -52,9 +52,10 @@ def _expected(jobs):
                                                 precision=j.precision).unbind(0)] for j in jobs]
 
 
+@pytest.mark.parametrize("staging", ["tma", "ldg"])
 @pytest.mark.parametrize("ctas", [0, 1, 2])
-def test_persistent_batch_matches_per_frame_launches(ctas):
-    jobs = _jobs()
+def test_persistent_batch_matches_per_frame_launches(ctas, staging):
+    jobs = _jobs(staging=staging)
     want = _expected(jobs)
     b = B.Batch(jobs, ctas_per_sm=ctas)
     b.launch()
@@ -116,7 +117,7 @@ def test_ragged_random_batches_match_per_frame_launches():
             dt = torch.float16
         osz = (W + int(rng.integers(1, 50)), H + int(rng.integers(1, 30))) if hm.family == "zoom" else None
         x = torch.from_numpy(synth.frame(H, W, 900 + i, hm.channels)).to("cuda", dt)
-        jobs.append(B.Job.make(hm, x, out_size=osz, precision=prec))
+        jobs.append(B.Job.make(hm, x, out_size=osz, precision=prec, staging=["tma", "ldg"][i % 2]))
     want = _expected(jobs)
     b = B.Batch(jobs)
     b.launch()
@@ -124,3 +125,28 @@ def test_ragged_random_batches_match_per_frame_launches():
     for j, w in zip(jobs, want):
         for o, e in zip(j.outputs, w):
             assert torch.equal(o, e), (j.model.name, j.precision, tuple(j.inputs[0].shape))
+
+
+def test_tma_staged_batches_of_larger_frames():
+    """Frames with many interior tiles, TMA-staged and clamped-load jobs
+    mixed in one persistent group (the CTAs switch tensor maps between jobs
+    and flip their mbarrier phase per TMA tile): per-frame pixels bit for bit."""
+    jobs = []
+    for i, (name, H, W, dt, prec) in enumerate([
+            ("ravu-lite-ar-r3", 120, 260, torch.float16, "fast"), ("ravu-lite-ar-r3", 97, 203, torch.float16, "fast"),
+            ("ravu-lite-ar-r3", 64, 150, torch.float16, "fast"), ("ravu-r3", 100, 200, torch.float32, "fp32"),
+            ("ravu-r3", 81, 131, torch.float32, "fp32"), ("ravu-3x-r3-rgb", 50, 90, torch.float16, "fast"),
+            ("ravu-3x-r3-rgb", 41, 77, torch.float16, "fast")]):
+        hm, _ = synth.model_for(name)
+        x = torch.from_numpy(synth.frame(H, W, 1200 + i, hm.channels)).to("cuda", dt)
+        jobs.append(B.Job.make(hm, x, precision=prec, staging=["tma", "ldg"][i % 2]))
+    want = _expected(jobs)
+    for ctas in (0, 1):
+        for j in jobs:
+            for o in j.outputs:
+                o.zero_()
+        B.Batch(jobs, ctas_per_sm=ctas).launch()
+        torch.cuda.synchronize()
+        for j, w in zip(jobs, want):
+            for o, e in zip(j.outputs, w):
+                assert torch.equal(o, e), (j.model.name, j.staging, ctas)

@@ -86,6 +86,17 @@ def test_job_make_shapes(name, shape, osz, want, scratch):
     assert j.out_size == (want[1], want[0])
 
 
+def test_job_staging_is_checked_and_keyed():
+    hm, _ = synth.model_for("ravu-lite-ar-r3")
+    x = torch.zeros((1, 36, 52), dtype=torch.float16)
+    assert B.Job.make(hm, x).staging == "tma"
+    assert B.STAGINGS[B.Job.make(hm, x, staging="ldg").staging] == 0
+    with pytest.raises(ValueError):
+        B.Job.make(hm, x, staging="texture")
+    a, b = B.Job.make(hm, x), B.Job.make(hm, x, staging="ldg")
+    assert B.PlanCache.key("GB300", [a]) != B.PlanCache.key("GB300", [b])
+
+
 # ----------------------------------------------- request sizing / admission --
 
 def test_request_bytes():
