@@ -53,6 +53,13 @@ class HookModel:
         self.model = model
         self._dev: Dict[int, int] = {}
         self._lock = threading.Lock()
+        # device work buffers of host pipelines, per (device, bytes), each
+        # with the completion event of its last call: a buffer is handed out
+        # again only after that event has passed, and never goes back to the
+        # caching allocator meanwhile, so it is idle when a call starts (its
+        # copies run on the library's copy streams, which the allocator does
+        # not track)
+        self._host_work: Dict[Tuple[int, int], List[Tuple["torch.cuda.Event", "torch.Tensor"]]] = {}
 
     # ---- metadata -----------------------------------------------------
     @property
@@ -346,19 +353,42 @@ class HookModel:
         h = self.device_handle(dev.index)
         with torch.cuda.device(dev):
             s = stream if stream is not None else torch.cuda.current_stream(dev)
-            nbytes = L.pz_run_host_work_bytes(h, W, H, dt, _ffi.ctypes.byref(o))
-            # a fresh block of the caching allocator: idle, and kept from reuse
-            # until the stream has passed this call (record_stream below)
-            work = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=dev)
-            _ffi.check(L.pz_run_host(h, frames.data_ptr(), out.data_ptr(), N, W, H, dt, _ffi.ctypes.byref(o),
-                                     work.data_ptr(), work.numel(), _ffi.PZ_HOST_WORK_IDLE, s.cuda_stream))
-            work.record_stream(s)
+            nbytes = max(int(L.pz_run_host_work_bytes(h, W, H, dt, _ffi.ctypes.byref(o))), 256)
+            work = self._take_host_work(dev, nbytes)   # idle: the copies may start at once
+            try:
+                _ffi.check(L.pz_run_host(h, frames.data_ptr(), out.data_ptr(), N, W, H, dt,
+                                         _ffi.ctypes.byref(o), work.data_ptr(), work.numel(),
+                                         _ffi.PZ_HOST_WORK_IDLE, s.cuda_stream))
+            finally:
+                fin = torch.cuda.Event()
+                fin.record(s)
+                self._give_host_work(dev, nbytes, fin, work)
             if wait:
-                s.synchronize()
+                fin.synchronize()
                 return out
-            fin = torch.cuda.Event()
-            fin.record(s)
             return out, fin
+
+    _HOST_WORK_KEEP = 8   # idle buffers kept per (device, size)
+
+    def _take_host_work(self, dev, nbytes: int):
+        torch = _torch()
+        with self._lock:
+            pool = self._host_work.setdefault((dev.index, nbytes), [])
+            for k, (ev, w) in enumerate(pool):
+                if ev.query():
+                    del pool[k]
+                    return w
+        return torch.empty(nbytes, dtype=torch.uint8, device=dev)
+
+    def _give_host_work(self, dev, nbytes: int, ev, work) -> None:
+        with self._lock:
+            pool = self._host_work.setdefault((dev.index, nbytes), [])
+            pool.append((ev, work))
+            while len(pool) > self._HOST_WORK_KEEP:   # drop the oldest finished buffer
+                k = next((i for i, (e, _) in enumerate(pool) if e.query()), None)
+                if k is None:
+                    break
+                del pool[k]
 
     def key_shape(self, W, H, OW, OH):
         fam = self.family

@@ -44,6 +44,31 @@ def test_host_pipelines_of_two_models_overlap_and_match():
         assert torch.equal(yb[i], b.upscale(frames[i].cuda(), precision="fast").cpu())
 
 
+def test_host_pipelines_of_one_model_back_to_back_match():
+    """Several wait=False calls of one model and frame size in flight
+    together: each call gets a work buffer no queued call still uses (its
+    copies start at once, on the library's copy streams), and finished
+    buffers are handed out again."""
+    hm, _ = synth.model_for("ravu-lite-ar-r3")
+    sets = [torch.stack([torch.from_numpy(synth.luma_plane(192, 320, 500 + 10 * k + i))[None] for i in range(6)])
+            .to(torch.float16).pin_memory() for k in range(3)]
+    keys0 = set(hm._host_work)
+    res = [hm.upscale_host(f, precision="fast", wait=False) for f in sets]
+    for f, (y, ev) in zip(sets, res):
+        ev.synchronize()
+        for i in range(6):
+            assert torch.equal(y[i], hm.upscale(f[i].cuda(), precision="fast").cpu())
+    (key,) = set(hm._host_work) - keys0
+    pool = hm._host_work[key]
+    # one buffer per call still in flight when the next was queued (how many
+    # overlapped depends on timing), never one buffer twice
+    assert 1 <= len(pool) <= 3 and len({w.data_ptr() for _, w in pool}) == len(pool)
+    n = len(pool)
+    y = hm.upscale_host(sets[0], precision="fast")       # reuses a finished buffer
+    assert len(hm._host_work[key]) == n
+    assert torch.equal(y, res[0][0])
+
+
 def test_host_pipeline_c_abi_checks_work_and_layout():
     import ctypes
     from mpv_prescalers_gb300 import _ffi, PrescaleError
