@@ -147,8 +147,9 @@ def resample_plane(x, out_w: int, out_h: int, sx: float, ox: float, sy: float, o
         raise ValueError("planes must be float32 or float16")
     if filt not in FILTERS:
         raise ValueError(f"filter {filt!r} not in {sorted(FILTERS)}")
-    if out is None:
-        out = torch.empty((out_h, out_w), dtype=x.dtype, device=x.device)
+    if out is None:   # allocated on the stream that writes it
+        with torch.cuda.device(x.device), torch.cuda.stream(stream):
+            out = torch.empty((out_h, out_w), dtype=x.dtype, device=x.device)
     dt = _ffi.PZ_F32 if x.dtype == torch.float32 else _ffi.PZ_F16
     pin = _ffi.Plane(x.data_ptr(), x.shape[1], x.shape[0], x.stride(0), dt)
     pout = _ffi.Plane(out.data_ptr(), out.shape[1], out.shape[0], out.stride(0), dt)

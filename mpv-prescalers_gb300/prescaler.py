@@ -272,13 +272,15 @@ class HookModel:
         torch = _torch()
         if not isinstance(planes, (list, tuple)) and planes.dim() == 4:
             # a batch of frames [N][C][H][W]: one chain per frame, same stream
-            outs = [self.upscale(f, out_size=out_size, precision=precision,
-                                 out=None if out is None else out[i], return_keys=return_keys, stream=stream,
-                                 staging=staging)
-                    for i, f in enumerate(planes.unbind(0))]
-            if return_keys:
-                return torch.stack([o[0] for o in outs]), torch.stack([o[1] for o in outs])
-            return torch.stack(outs) if out is None else out
+            # (the results are gathered on that stream, after the kernels)
+            with torch.cuda.stream(stream):
+                outs = [self.upscale(f, out_size=out_size, precision=precision,
+                                     out=None if out is None else out[i], return_keys=return_keys, stream=stream,
+                                     staging=staging)
+                        for i, f in enumerate(planes.unbind(0))]
+                if return_keys:
+                    return torch.stack([o[0] for o in outs]), torch.stack([o[1] for o in outs])
+                return torch.stack(outs) if out is None else out
         as_list = isinstance(planes, (list, tuple))
         pl = list(planes) if as_list else ([planes] if planes.dim() == 2 else list(planes.unbind(0)))
         if len(pl) != self.n_planes:
@@ -298,9 +300,13 @@ class HookModel:
             return self._pack(res, planes, as_list, None, return_keys)
         OW, OH = self.output_size(W, H, out_size)
         dev = pl[0].device
-        with torch.cuda.device(dev):
+        # results are allocated (and packed) on the stream that writes them,
+        # so the caching allocator orders their reuse after the kernels
+        with torch.cuda.device(dev), torch.cuda.stream(stream):
+            full = None
             if out is None:
-                res = [torch.empty((OH, OW), dtype=pl[0].dtype, device=dev) for _ in pl]
+                full = torch.empty((len(pl), OH, OW), dtype=pl[0].dtype, device=dev)
+                res = list(full.unbind(0))
             else:
                 res = list(out) if isinstance(out, (list, tuple)) else ([out] if out.dim() == 2 else list(out.unbind(0)))
             keys = None
@@ -308,7 +314,7 @@ class HookModel:
                 keys = torch.empty(self.key_shape(W, H, OW, OH), dtype=torch.int32, device=dev)
             self.run_raw(pl, res, out_size=(OW, OH), precision=precision, keys=keys, stream=stream,
                          staging=staging)
-        return self._pack(res, planes, as_list, keys, return_keys)
+            return self._pack(res, planes, as_list, keys, return_keys, full)
 
     def upscale_host(self, frames, out=None, out_size: Optional[Tuple[int, int]] = None, precision: str = "fp32",
                      device=None, wait: bool = True, stream=None):
@@ -427,12 +433,16 @@ class HookModel:
         _ffi.check(_ffi.lib().pz_run(h, pin, n, pout, n, _ffi.ctypes.byref(o), s.cuda_stream))
 
     @staticmethod
-    def _pack(res, planes, as_list, keys, return_keys):
+    def _pack(res, planes, as_list, keys, return_keys, full=None):
+        """The results in the input's form; ``full``: the [C][OH][OW] tensor
+        whose planes ``res`` are, when the results were allocated here."""
         torch = _torch()
         if as_list:
             r = res
         elif planes.dim() == 2:
             r = res[0]
+        elif full is not None:
+            r = full
         else:
             r = torch.stack(res) if len(res) > 1 else res[0].unsqueeze(0)
         return (r, keys) if return_keys else r

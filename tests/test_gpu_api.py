@@ -69,6 +69,25 @@ def test_host_pipelines_of_one_model_back_to_back_match():
     assert torch.equal(y, res[0][0])
 
 
+@pytest.mark.parametrize("shape", [(3, 240, 320), (2, 3, 120, 160)], ids=["planes", "batch"])
+def test_upscale_on_a_side_stream(shape):
+    """With ``stream=`` the results are allocated and gathered on that stream
+    (the [C][H][W] result is one tensor whose planes the kernels write; a
+    batch is stacked after its kernels), so they equal the default-stream run."""
+    hm, _ = synth.model_for("ravu-r3-yuv")
+    x = torch.from_numpy(np.stack([synth.frame(shape[-2], shape[-1], 700 + i, hm.channels)
+                                   for i in range(shape[0] if len(shape) == 4 else 1)]))
+    x = (x if len(shape) == 4 else x[0]).to("cuda", torch.float16)
+    want = hm.upscale(x, precision="fast")
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    got = hm.upscale(x, precision="fast", stream=s)
+    s.synchronize()
+    assert got.shape == want.shape and got.is_contiguous()
+    assert torch.equal(got, want)
+
+
 def test_host_pipeline_c_abi_checks_work_and_layout():
     import ctypes
     from mpv_prescalers_gb300 import _ffi, PrescaleError
