@@ -22,9 +22,11 @@ Reported (one JSON line on rank 0):
 * ``headline``: chosen vs plain FP32 Mpix/s for ravu-lite-ar-r3 and
   nnedi3-nns128-win8x6 on 1920x1080 -> 3840x2160.
 
-``--impl reference`` times the reference arm: the CPU restatement of the
-shader arithmetic (the reference's shaders need an OpenGL/Vulkan host that
-this machine does not have), on all host cores, same metric and workload.
+``--impl reference`` times the reference arm on all host cores, same metric
+and workload: the reference's shader text compiled as FP64 C++ and run
+through the hook host's pass sequence (``oracle/_ref``, compiled by
+``build()``; the shaders themselves need an OpenGL/Vulkan host that this
+machine does not have), else the FP64 NumPy restatement of its arithmetic.
 """
 from __future__ import annotations
 
@@ -59,6 +61,29 @@ def _pkg():
 
 # ------------------------------------------------------------------ CPU ---
 
+_FRAME = {}   # per worker process: the synthetic frame of each seed, made before timing
+
+
+def _frame(seed: int):
+    if seed not in _FRAME:
+        from mpv_prescalers_gb300 import synth
+        _FRAME[seed] = synth.luma_plane(H, W, seed)
+    return _FRAME[seed]
+
+
+def _worker_init(seed: int, kind: str):
+    """Pool initializer: package, frame and (reference) compiled shaders are
+    ready before the timed strips start."""
+    sys.path.insert(0, REPO)
+    _pkg()
+    _frame(seed)
+    if kind == "reference":
+        for n in MODELS:
+            _ref_strip((n, 0, 8, seed))       # loads the shader library and its LUT textures
+    else:
+        import oracle  # noqa: F401
+
+
 def _cpu_strip(args):
     """Oracle on rows [y0, y1) of one frame (with the window halo)."""
     name, y0, y1, seed = args
@@ -67,7 +92,7 @@ def _cpu_strip(args):
     from mpv_prescalers_gb300 import synth
     import oracle
     hm, _ = synth.model_for(name)
-    x = synth.luma_plane(H, W, seed)
+    x = _frame(seed)
     pad = 6  # covers the windows: lite r4 +-3, ravu r3 int11 (+-3) feeding the lattice (+-3)
     a, b = max(0, y0 - pad), min(H, y1 + pad)
     t = time.perf_counter()
@@ -76,24 +101,78 @@ def _cpu_strip(args):
     return (y1 - y0) * W * 4, dt
 
 
-def cpu_baseline(rows_per_model: int, workers: int):
-    """Oracle Mpix/s on a bounded sample: `rows_per_model` input rows of frame
-    0 per model, split in strips over `workers` spawned processes."""
+_REF_LIBS = {}
+
+
+def _ref_lib(name: str):
+    """The reference's own shader text for `name`, compiled for this machine
+    (oracle/_ref, built by build()), or None."""
+    import ctypes
+    if name not in _REF_LIBS:
+        path = os.path.join(REPO, "oracle", "_ref", name + ".so")
+        lib = None
+        if os.path.exists(path):
+            try:
+                lib = ctypes.CDLL(path)
+                lib.ref_run.restype = ctypes.c_int
+            except OSError:
+                lib = None
+        _REF_LIBS[name] = lib
+    return _REF_LIBS[name]
+
+
+def _ref_strip(args):
+    """The compiled reference shaders on rows [y0, y1) of one frame (with the
+    window halo): every pass of the file per pixel, as the hook host runs it."""
+    import ctypes
+    name, y0, y1, seed = args
+    sys.path.insert(0, REPO)
+    _pkg()
+    from mpv_prescalers_gb300 import synth
+    lib = _ref_lib(name)
+    x = _frame(seed)
+    pad = 6
+    a, b = max(0, y0 - pad), min(H, y1 + pad)
+    xin = np.ascontiguousarray(x[a:b], dtype=np.float64)
+    h = b - a
+    out = np.empty(4 * h * W)
+    dims = (ctypes.c_int * 2)()
+    t = time.perf_counter()
+    rc = lib.ref_run(xin.ctypes.data_as(ctypes.c_void_p), 1, h, W, 2 * W, 2 * h,
+                     out.ctypes.data_as(ctypes.c_void_p), out.size, dims)
+    dt = time.perf_counter() - t
+    if rc != 0 or (dims[0], dims[1]) != (2 * h, 2 * W):
+        raise RuntimeError(f"reference {name}: ref_run {rc}, dims {dims[0]}x{dims[1]}")
+    return (y1 - y0) * W * 4, dt
+
+
+def reference_available() -> bool:
+    return all(_ref_lib(n) is not None for n in MODELS)
+
+
+def cpu_baseline(rows_per_model: int, workers: int, kind: str = "port"):
+    """CPU Mpix/s on a bounded sample: `rows_per_model` input rows of frame 0
+    per model, split in strips over `workers` spawned processes; `kind`
+    "port" runs the FP64 NumPy oracle, "reference" the reference's shader
+    text compiled as C++ (oracle/_ref)."""
     ctx = mp.get_context("spawn")
+    fn = _ref_strip if kind == "reference" else _cpu_strip
     tasks = []
     strip = max(8, rows_per_model // workers)
     for name in MODELS:
         for y0 in range(0, rows_per_model, strip):
             tasks.append((name, y0, min(rows_per_model, y0 + strip), SEED0))
-    with ctx.Pool(workers) as pool:
-        pool.map(_cpu_strip, [(MODELS[0], 0, 8, SEED0)] * workers)  # warm the workers
+    with ctx.Pool(workers, initializer=_worker_init, initargs=(SEED0, kind)) as pool:
+        pool.map(fn, [(n, 0, 8, SEED0) for n in MODELS] * workers)  # warm the workers
         t = time.perf_counter()
-        res = pool.map(_cpu_strip, tasks)
+        res = pool.map(fn, tasks)
         wall = time.perf_counter() - t
     px = sum(r[0] for r in res)
-    return {"value": px / wall / 1e6, "unit": "Mpix/s", "cores": workers, "kind": "port",
+    what = ("the reference's shader text compiled as FP64 C++ (every pass per pixel, as the hook host runs it)"
+            if kind == "reference" else "FP64 NumPy oracle")
+    return {"value": px / wall / 1e6, "unit": "Mpix/s", "cores": workers, "kind": kind,
             "sample": f"{rows_per_model} of {H} input rows of one 1920x1080 frame per model "
-                      f"({', '.join(MODELS)}), FP64 NumPy oracle, {len(tasks)} strips on {workers} processes",
+                      f"({', '.join(MODELS)}), {what}, {len(tasks)} strips on {workers} processes",
             "seconds": wall}
 
 
@@ -453,16 +532,19 @@ def run_reference(args):
     if rank != 0:
         return None
     workers = len(os.sched_getaffinity(0))
+    # the reference's own shader text compiled for this machine when build()
+    # made it, else the NumPy restatement of its arithmetic
+    kind = "reference" if reference_available() else "port"
     # each step is a bounded sample: rows per step are sized from a calibration
     # run so that all steps together take about `ref_budget` seconds
-    calib = cpu_baseline(2 * workers, workers)
+    calib = cpu_baseline(2 * workers, workers, kind)
     rows_per_s = 2 * workers * len(MODELS) / max(calib["seconds"], 1e-3) / len(MODELS)
     rows = int(max(16, min(args.ref_rows, args.ref_budget / max(args.steps, 1) * rows_per_s)))
     for _ in range(max(0, min(args.warmup, 1))):
-        cpu_baseline(16, workers)
+        cpu_baseline(16, workers, kind)
     vals = []
     for _ in range(args.steps):
-        vals.append(cpu_baseline(rows, workers))
+        vals.append(cpu_baseline(rows, workers, kind))
     v = statistics.mean(r["value"] for r in vals)
     cb = dict(vals[-1])
     cb["value"] = v
@@ -474,8 +556,9 @@ def run_reference(args):
             "config": {"workload": "8x 1920x1080 FP16 luma -> 3840x2160 through ravu-lite-ar-r4 and ravu-r3",
                        "sample": cb["sample"]},
             "cpu_baseline": cb, "e2e": {"value": v, "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "reference shaders need mpv + OpenGL/Vulkan (unavailable on this box); the reference arm is "
-                    "the CPU restatement of their arithmetic (FP64 NumPy), all host cores"}
+            "note": "the reference's shaders need mpv + OpenGL/Vulkan (unavailable on this box); the reference "
+                    "arm runs their GLSL bodies compiled as FP64 C++ (oracle/_ref) through the hook host's pass "
+                    "sequence when build() compiled them here, else the FP64 NumPy restatement, all host cores"}
 
 
 # Single-kernel cases for profilers: (model, channels of the frame, out_size,
@@ -543,7 +626,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-rows", type=int, default=1080, help="input rows per model in the CPU sample")
-    ap.add_argument("--ref-rows", type=int, default=540, help="largest CPU sample per reference step (input rows)")
+    ap.add_argument("--ref-rows", type=int, default=1080, help="largest CPU sample per reference step (input rows)")
     ap.add_argument("--ref-budget", type=float, default=90.0, help="seconds of CPU work for all reference steps")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=480, help="requests in the serving trace (0: skip)")

@@ -22,6 +22,11 @@ place, never copied into the repository) this script
 Outputs go only to ``oracle/_ref/`` (git-ignored).  Usage::
 
     python oracle/build_ref.py [--ref /root/reference] [names...]
+    python oracle/build_ref.py --generated [names...]
+
+``--generated`` compiles the C++ this recipe already wrote into
+``oracle/_ref/`` (for a machine of another architecture that received the
+generated sources but not the reference checkout); nothing is regenerated.
 """
 from __future__ import annotations
 
@@ -209,11 +214,44 @@ def build_one(ref: str, stem: str) -> str:
     return so
 
 
+def compile_generated(names) -> list:
+    """Compile generated ``oracle/_ref/<name>.cpp`` files (and ``rpn.cpp``)
+    whose shared library is missing or older than the source."""
+    def stale(src, dst):
+        return not os.path.exists(dst) or os.path.getmtime(dst) < os.path.getmtime(src)
+    rpn_cpp, rpn_o = os.path.join(OUT, "rpn.cpp"), os.path.join(OUT, "rpn.o")
+    if not os.path.exists(rpn_cpp):
+        return []
+    if stale(rpn_cpp, rpn_o):
+        subprocess.run(["g++", "-std=c++17", "-O1", "-fPIC", "-c", f"-I{HERE}", "-o", rpn_o, rpn_cpp], check=True)
+    todo = []
+    for stem in names:
+        cpp, so = os.path.join(OUT, stem + ".cpp"), os.path.join(OUT, stem + ".so")
+        if os.path.exists(cpp) and (stale(cpp, so) or stale(rpn_o, so)):
+            todo.append((cpp, so))
+
+    def one(job):
+        cpp, so = job
+        subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fPIC", "-shared", "-w",
+                        f"-I{HERE}", "-o", so, cpp, rpn_o], check=True)
+        return so
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        return list(ex.map(one, todo))
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=DEFAULT_REF)
+    ap.add_argument("--generated", action="store_true",
+                    help="compile the C++ already generated under oracle/_ref (no reference needed)")
     ap.add_argument("names", nargs="*")
     a = ap.parse_args(argv)
+    if a.generated:
+        names = a.names or sorted(fn[:-4] for fn in os.listdir(OUT) if fn.endswith(".cpp") and fn != "rpn.cpp") \
+            if os.path.isdir(OUT) else []
+        for so in compile_generated(names):
+            print("built", os.path.relpath(so, HERE))
+        return 0
     if not os.path.isdir(a.ref):
         print(f"reference not present at {a.ref}; nothing to build")
         return 0
