@@ -110,6 +110,10 @@ class Batch:
         torch = _torch()
         s = stream if stream is not None else torch.cuda.current_stream(self.device)
         _ffi.check(_ffi.lib().pz_batch_launch(self._plan, s.cuda_stream))
+        if not torch.cuda.is_current_stream_capturing():
+            # the job table and counters must outlive this launch even if the
+            # plan is dropped first (a no-op on the stream they came from)
+            self.work.record_stream(s)
 
     def capture(self):
         """Record one launch into a CUDA graph (call launch() once first so

@@ -213,10 +213,16 @@ __device__ __forceinline__ void ar_pow2(float v, float2& p32, float2& p33) {
 
 // lo = 1.1 - lo2/lo; hi = hi2/hi - 0.1; mix(res, clamp(res, lo, hi), s).
 // The quotients are approximate (__fdividef, about 2 ulp, the precision a
-// shader's division has): they only move the clamp bounds, by < 3e-7.
+// shader's division has): they only move the clamp bounds, by < 3e-7.  Both
+// operands are scaled by 2^24 first, so that a subnormal denominator
+// (positive weights summing below ~1e-6) still has a finite reciprocal; for
+// every other denominator the scaling changes no bit of the quotient.
+__device__ __forceinline__ float ar_quot(float n, float d) {
+  return __fdividef(n * 16777216.0f, d * 16777216.0f);
+}
 __device__ __forceinline__ float ar_finish(float res, float lo, float hi, float lo2, float hi2, float s) {
-  float lob = 1.1f - __fdividef(lo2, lo);
-  float hib = __fdividef(hi2, hi) - 0.1f;
+  float lob = 1.1f - ar_quot(lo2, lo);
+  float hib = ar_quot(hi2, hi) - 0.1f;
   float c = fminf(fmaxf(res, lob), hib);
   return res * (1.0f - s) + c * s;
 }
