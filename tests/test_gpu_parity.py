@@ -308,3 +308,26 @@ def test_empty_planes_are_rejected():
     x = torch.empty((0, 30), device="cuda")
     with pytest.raises((PrescaleError, ValueError)):
         hm.upscale(x)
+
+
+@pytest.mark.parametrize("name,zoom", [("ravu-lite-ar-r2", False), ("ravu-lite-ar-r3", False),
+                                       ("ravu-zoom-ar-r2", True)])
+def test_anti_ringing_with_subnormal_weight_sums(name, zoom):
+    """Anti-ringing where the clamp bounds' denominators are subnormal: tiny
+    positive LUT weights (1e-7) on a white plane give sum(w * (1.1 - 1)^32)
+    ~ 1e-39.  The bounds are still finite (lo = hi = 1), as in the oracle."""
+    import dataclasses
+    from mpv_prescalers_gb300.prescaler import HookModel
+    base = _model(name)
+    lut = np.full_like(base.model.lut, 1e-7)
+    kw = {"lut": lut}
+    if zoom:
+        kw["lut_ar"] = np.full_like(base.model.lut_ar, 1e-7)
+    hm = HookModel(dataclasses.replace(base.model, **kw))
+    x = np.ones((1, 24, 40), dtype=np.float32)
+    out_size = (60, 36) if zoom else None
+    y, kg = _run_gpu(hm, x, out_size)
+    forced, _ = oracle.keyed_upscale(hm.model, x, out_size, keys=kg)
+    assert np.isfinite(y).all()
+    assert np.abs(y - forced).max() <= TOL_FP32
+    assert np.abs(y - 0.8).max() < 1e-3       # 0.2 * (sum of tiny weights) + 0.8 * 1
