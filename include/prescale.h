@@ -190,12 +190,15 @@ typedef struct {
 
 /* Many frames of many models per launch (replaces the back-to-back shader
  * dispatches a multi-stream host issues).  RAVU jobs of any mix and frame
- * size run as one persistent kernel per plane dtype whose CTAs pull 32x8
- * tiles of every job from a device counter; the ravu lattice pass follows as
- * a second persistent kernel (it reads the int11 values of the first);
- * NNEDI3 jobs run as their own stream-ordered passes.  `work` is caller
- * device memory of at least pz_batch_work_bytes(); it holds the job table
- * and the tile counters and must stay in place while the plan is used.
+ * size run as one persistent kernel per tile program and plane dtype whose
+ * CTAs pull 32x8 tiles of every job of that program from a device counter;
+ * the ravu lattice passes follow as second-phase kernels (they read the
+ * int11 values of the first); NNEDI3 jobs run as their own stream-ordered
+ * passes.  A job whose opts.staging is 1 has its interior tiles staged by
+ * TMA inside the persistent loop too (its tensor maps sit in the job table).
+ * `work` is caller device memory of at least pz_batch_work_bytes(); it
+ * holds the job table and the tile counters and must stay in place while
+ * the plan is used.
  *
  * pz_batch_create validates the jobs and uploads the table (synchronous on
  * `cuda_stream`); pz_batch_launch only enqueues a memset and kernels, so it
