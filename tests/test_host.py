@@ -218,6 +218,41 @@ def test_bench_replica_timing_single_process():
     assert bench.job_value(2e6, 10, 1000.0, 1) == pytest.approx(20.0)
 
 
+@pytest.mark.parametrize("kind", ["port", "reference"])
+def test_bench_cpu_baseline_kinds(kind):
+    """The CPU legs of bench.py on a small sample: the NumPy oracle ("port")
+    and the reference's shader text compiled as C++ ("reference", when
+    build() made oracle/_ref here)."""
+    import bench
+    if kind == "reference" and not bench.reference_available():
+        pytest.skip("oracle/_ref not built on this machine")
+    r = bench.cpu_baseline(16, 2, kind)
+    assert r["kind"] == kind and r["cores"] == 2 and r["value"] > 0 and r["unit"] == "Mpix/s"
+    assert "16 of 1080 input rows" in r["sample"]
+
+
+def test_bench_reference_strip_matches_the_oracle():
+    """One strip of the compiled reference shaders equals the NumPy oracle on
+    the same rows (the two CPU legs compute the same pixels)."""
+    import ctypes
+    import bench
+    if not bench.reference_available():
+        pytest.skip("oracle/_ref not built on this machine")
+    import oracle
+    hm, src = synth.model_for("ravu-lite-ar-r4")
+    if src != "parsed":
+        pytest.skip("the model cache (the reference's own LUTs) is not present")
+    x = synth.luma_plane(20, 48, 77).astype(np.float64)
+    lib = bench._ref_lib("ravu-lite-ar-r4")
+    out = np.empty(4 * x.size)
+    dims = (ctypes.c_int * 2)()
+    assert lib.ref_run(x.ctypes.data_as(ctypes.c_void_p), 1, 20, 48, 96, 40,
+                       out.ctypes.data_as(ctypes.c_void_p), out.size, dims) == 0
+    assert (dims[0], dims[1]) == (40, 96)
+    want, _ = oracle.keyed_upscale(hm.model, x[None].astype(np.float32))
+    assert np.abs(out.reshape(40, 96) - want[0]).max() < 1e-9
+
+
 def test_trace_output_rings_are_per_stream_and_shaped():
     models = _trace_models()
     res = ((64, 36, 0.5), (96, 54, 0.5))
