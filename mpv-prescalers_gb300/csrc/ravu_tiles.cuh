@@ -17,6 +17,7 @@
 // t handles column t % 32 of row t / 32.  Out-of-range reads replicate the
 // edge texel (the mpv texture border mode).
 #pragma once
+#include <cstddef>
 #include <cstring>
 
 #include "async.cuh"
@@ -800,6 +801,8 @@ struct DevJob {
   int has_maps;
   TmaMaps maps;    // 64-byte aligned (CUtensorMap)
 };
+// every job's maps start on a 64-byte boundary of the (256-byte aligned) table
+static_assert(sizeof(DevJob) % 64 == 0 && offsetof(DevJob, maps) % 64 == 0, "tensor maps must be 64-byte aligned");
 
 // Persistent CTAs of one tile program: claim tile numbers from `counter`
 // until `total`; a tile's job is the last whose first tile <= the number
