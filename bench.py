@@ -644,8 +644,9 @@ def main():
             print(json.dumps(line))
         return
     rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     cb = None
-    if rank == 0 and not args.no_cpu:  # the CPU pool starts before any GPU call
+    if rank == 0 and world == 1 and not args.no_cpu:  # the CPU pool starts before any GPU call
         cb = cpu_baseline(args.cpu_rows, len(os.sched_getaffinity(0)))
     line = run_gpu(args)
     if line is not None:
