@@ -217,18 +217,29 @@ def build_one(ref: str, stem: str) -> str:
 def compile_generated(names) -> list:
     """Compile generated ``oracle/_ref/<name>.cpp`` files (and ``rpn.cpp``)
     whose shared library is missing or older than the source."""
+    def loads(so):  # a library built for another machine does not load here
+        import ctypes
+        try:
+            ctypes.CDLL(so)
+            return True
+        except OSError:
+            return False
+
     def stale(src, dst):
         return not os.path.exists(dst) or os.path.getmtime(dst) < os.path.getmtime(src)
     rpn_cpp, rpn_o = os.path.join(OUT, "rpn.cpp"), os.path.join(OUT, "rpn.o")
     if not os.path.exists(rpn_cpp):
         return []
-    if stale(rpn_cpp, rpn_o):
-        subprocess.run(["g++", "-std=c++17", "-O1", "-fPIC", "-c", f"-I{HERE}", "-o", rpn_o, rpn_cpp], check=True)
     todo = []
     for stem in names:
         cpp, so = os.path.join(OUT, stem + ".cpp"), os.path.join(OUT, stem + ".so")
-        if os.path.exists(cpp) and (stale(cpp, so) or stale(rpn_o, so)):
+        if os.path.exists(cpp) and (stale(cpp, so) or not loads(so)):
             todo.append((cpp, so))
+    if not todo:
+        return []
+    # rpn.o is rebuilt with them: an object carried over from another
+    # machine cannot be told apart by its timestamp
+    subprocess.run(["g++", "-std=c++17", "-O1", "-fPIC", "-c", f"-I{HERE}", "-o", rpn_o, rpn_cpp], check=True)
 
     def one(job):
         cpp, so = job
