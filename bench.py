@@ -21,6 +21,11 @@ Reported (one JSON line on rank 0):
   workload, on the host's cores.
 * ``headline``: chosen vs plain FP32 Mpix/s for ravu-lite-ar-r3 and
   nnedi3-nns128-win8x6 on 1920x1080 -> 3840x2160.
+* ``precision``: per configuration, the GPU output against the FP64 oracle
+  on the same input (the outputs the ``cpu_baseline`` leg computed): max-abs,
+  PSNR and, for RAVU, the LUT-key mismatch and boundary rates (frame 0 of the
+  bench batch in the chosen form; ravu-lite-r3 on 960x540 in plain FP32;
+  nnedi3-nns128-win8x6 on 1280x720 in both forms).
 
 ``--impl reference`` times the reference arm on all host cores, same metric
 and workload: the reference's shader text compiled as FP64 C++ and run
@@ -64,11 +69,15 @@ def _pkg():
 _FRAME = {}   # per worker process: the synthetic frame of each seed, made before timing
 
 
-def _frame(seed: int):
-    if seed not in _FRAME:
+def _frame(seed: int, h: int = H, w: int = W, fp16: bool = True):
+    """The synthetic luma plane of `seed`; fp16: rounded to FP16, the values
+    the chosen form's FP16 planes hold (the bench batch is stored FP16)."""
+    k = (seed, h, w, fp16)
+    if k not in _FRAME:
         from mpv_prescalers_gb300 import synth
-        _FRAME[seed] = synth.luma_plane(H, W, seed)
-    return _FRAME[seed]
+        x = synth.luma_plane(h, w, seed)
+        _FRAME[k] = x.astype(np.float16).astype(np.float32) if fp16 else x
+    return _FRAME[k]
 
 
 def _worker_init(seed: int, kind: str):
@@ -85,20 +94,33 @@ def _worker_init(seed: int, kind: str):
 
 
 def _cpu_strip(args):
-    """Oracle on rows [y0, y1) of one frame (with the window halo)."""
-    name, y0, y1, seed = args
+    """Oracle on rows [y0, y1) of one frame (with the window halo); returns
+    (output pixels, seconds, payload).  With `keep` the payload holds the
+    strip's FP64 outputs (as FP32), and for RAVU its keys, boundary flags
+    and key margins, for the precision check of the GPU run."""
+    name, y0, y1, seed, h, w, fp16, keep = args
     sys.path.insert(0, REPO)
-    pkg = _pkg()
+    _pkg()
     from mpv_prescalers_gb300 import synth
     import oracle
     hm, _ = synth.model_for(name)
-    x = _frame(seed)
-    pad = 6  # covers the windows: lite r4 +-3, ravu r3 int11 (+-3) feeding the lattice (+-3)
-    a, b = max(0, y0 - pad), min(H, y1 + pad)
+    x = _frame(seed, h, w, fp16)
+    pad = 6  # covers the windows: lite r4 +-3, ravu r3 int11 (+-3) feeding the lattice (+-3), nnedi3 +-5
+    a, b = max(0, y0 - pad), min(h, y1 + pad)
     t = time.perf_counter()
-    y, _ = oracle.keyed_upscale(hm.model, x[a:b])
+    if hm.family == "nnedi3":
+        y, info = oracle.nnedi3_upscale(hm.model, x[a:b])
+    else:
+        y, info = oracle.keyed_upscale(hm.model, x[a:b][None])
     dt = time.perf_counter() - t
-    return (y1 - y0) * W * 4, dt
+    payload = None
+    if keep:
+        r0, r1 = y0 - a, y1 - a
+        payload = {"y0": y0, "out": np.asarray(y[..., 2 * r0:2 * r1, :], dtype=np.float32)}
+        if hm.family != "nnedi3":
+            payload.update({k: info[k][..., r0:r1, :] for k in ("key", "boundary")})
+            payload["margin"] = np.asarray(info["margin"][..., r0:r1, :], dtype=np.float32)
+    return (y1 - y0) * w * 4, dt, payload
 
 
 _REF_LIBS = {}
@@ -125,7 +147,7 @@ def _ref_strip(args):
     """The compiled reference shaders on rows [y0, y1) of one frame (with the
     window halo): every pass of the file per pixel, as the hook host runs it."""
     import ctypes
-    name, y0, y1, seed = args
+    name, y0, y1, seed = args[:4]
     sys.path.insert(0, REPO)
     _pkg()
     from mpv_prescalers_gb300 import synth
@@ -143,37 +165,70 @@ def _ref_strip(args):
     dt = time.perf_counter() - t
     if rc != 0 or (dims[0], dims[1]) != (2 * h, 2 * W):
         raise RuntimeError(f"reference {name}: ref_run {rc}, dims {dims[0]}x{dims[1]}")
-    return (y1 - y0) * W * 4, dt
+    return (y1 - y0) * W * 4, dt, None
 
 
 def reference_available() -> bool:
     return all(_ref_lib(n) is not None for n in MODELS)
 
 
-def cpu_baseline(rows_per_model: int, workers: int, kind: str = "port"):
+# The other configurations whose precision the bench line states: (label,
+# model, height, width, seed, FP16-rounded input).  Seeds: 1000 * the
+# configuration's number + frame.
+CHECKS = (("config1 ravu-lite-r3 960x540 fp32", "ravu-lite-r3", 540, 960, 1000, False),
+          ("config3 nnedi3-nns128-win8x6 1280x720 fp32", "nnedi3-nns128-win8x6", 720, 1280, 3000, False),
+          ("config3 nnedi3-nns128-win8x6 1280x720 fp16", "nnedi3-nns128-win8x6", 720, 1280, 3000, True))
+
+
+def _assemble(parts):
+    """Stack the kept strips of one plane (in row order) into whole arrays."""
+    parts = sorted((p for p in parts if p is not None), key=lambda p: p["y0"])
+    return {k: np.concatenate([p[k] for p in parts], axis=-2) for k in parts[0] if k != "y0"}
+
+
+def cpu_baseline(rows_per_model: int, workers: int, kind: str = "port", checks: bool = False):
     """CPU Mpix/s on a bounded sample: `rows_per_model` input rows of frame 0
-    per model, split in strips over `workers` spawned processes; `kind`
-    "port" runs the FP64 NumPy oracle, "reference" the reference's shader
-    text compiled as C++ (oracle/_ref)."""
+    of the bench batch (FP16-rounded, the values the chosen form reads) per
+    model, split in strips over `workers` spawned processes; `kind` "port"
+    runs the FP64 NumPy oracle, "reference" the reference's shader text
+    compiled as C++ (oracle/_ref).
+
+    With `checks` (oracle only) it also returns the FP64 outputs it computed
+    -- frame 0 of each model, plus untimed oracle runs of the CHECKS
+    configurations -- as {label: arrays} for the precision figures of the
+    GPU run."""
     ctx = mp.get_context("spawn")
     fn = _ref_strip if kind == "reference" else _cpu_strip
+    keep = checks and kind == "port"
     tasks = []
     strip = max(8, rows_per_model // workers)
     for name in MODELS:
         for y0 in range(0, rows_per_model, strip):
-            tasks.append((name, y0, min(rows_per_model, y0 + strip), SEED0))
+            tasks.append((name, y0, min(rows_per_model, y0 + strip), SEED0, H, W, True, keep))
+    refs = {}
     with ctx.Pool(workers, initializer=_worker_init, initargs=(SEED0, kind)) as pool:
-        pool.map(fn, [(n, 0, 8, SEED0) for n in MODELS] * workers)  # warm the workers
+        pool.map(fn, [(n, 0, 8, SEED0, H, W, True, False) for n in MODELS] * workers)  # warm the workers
         t = time.perf_counter()
         res = pool.map(fn, tasks)
         wall = time.perf_counter() - t
+        if keep:
+            for name in MODELS:
+                refs[name] = _assemble([r[2] for r, tk in zip(res, tasks) if tk[0] == name])
+            extra = []
+            for label, name, h, w, seed, fp16 in CHECKS:
+                st = max(8, h // workers)
+                extra += [(label, (name, y0, min(h, y0 + st), seed, h, w, fp16, True)) for y0 in range(0, h, st)]
+            out = pool.map(fn, [e[1] for e in extra])
+            for label, *_ in CHECKS:
+                refs[label] = _assemble([o[2] for o, e in zip(out, extra) if e[0] == label])
     px = sum(r[0] for r in res)
     what = ("the reference's shader text compiled as FP64 C++ (every pass per pixel, as the hook host runs it)"
             if kind == "reference" else "FP64 NumPy oracle")
-    return {"value": px / wall / 1e6, "unit": "Mpix/s", "cores": workers, "kind": kind,
-            "sample": f"{rows_per_model} of {H} input rows of one 1920x1080 frame per model "
-                      f"({', '.join(MODELS)}), {what}, {len(tasks)} strips on {workers} processes",
-            "seconds": wall}
+    cb = {"value": px / wall / 1e6, "unit": "Mpix/s", "cores": workers, "kind": kind,
+          "sample": f"{rows_per_model} of {H} input rows of one 1920x1080 frame per model "
+                    f"({', '.join(MODELS)}), {what}, {len(tasks)} strips on {workers} processes",
+          "seconds": wall}
+    return (cb, refs) if checks else cb
 
 
 # ---------------------------------------------------------------- clocks ---
@@ -246,7 +301,67 @@ def job_value(out_px_per_rank_step: float, steps: int, ms: float, world: int) ->
     return world * out_px_per_rank_step * steps / (ms / 1e3) / 1e6
 
 
-def run_gpu(args):
+def _key_figures(kg, ref):
+    """Key agreement of a GPU run with the oracle's keys (arrays of the same
+    shape): mismatch and boundary rates, mismatches off the boundary, and the
+    largest margin (units of 2^-24 of the tensor scale) a flipped key had."""
+    kg = np.asarray(kg).reshape(ref["key"].shape)
+    mism = kg != ref["key"]
+    bnd = ref["boundary"]
+    marg = ref["margin"][mism] / 2.0 ** -24
+    return {"keys": int(mism.size), "key_mismatch_rate": float(mism.mean()), "boundary_rate": float(bnd.mean()),
+            "mismatch_off_boundary": int((mism & ~bnd).sum()),
+            "max_mismatch_margin_ulp": float(marg.max()) if marg.size else 0.0}
+
+
+def _value_figures(y, ref_out):
+    """max-abs and PSNR (peak 1.0) of GPU output rows against the oracle's."""
+    y = np.asarray(y, dtype=np.float64).reshape(ref_out.shape)
+    d = y - ref_out.astype(np.float64)
+    mse = float(np.mean(d * d))
+    return {"max_abs": float(np.abs(d).max()), "psnr_db": float("inf") if mse == 0 else 10 * np.log10(1 / mse)}
+
+
+def precision_figures(models, refs, dev):
+    """Per configuration: the GPU's output (and keys) against the FP64
+    outputs the CPU leg computed on the same inputs."""
+    import torch
+    from mpv_prescalers_gb300 import synth
+    figs = {}
+    for n in MODELS:  # frame 0 of the bench batch, chosen form, FP16 planes
+        ref = refs[n]
+        rows = ref["out"].shape[-2] // 2
+        x = torch.from_numpy(_frame(SEED0)).to(dev, torch.float16)
+        y, k = models[n].upscale(x, precision="fast", return_keys=True)
+        f = _value_figures(y.float().cpu().numpy()[..., :2 * rows, :], ref["out"])
+        k = k.cpu().numpy()
+        if k.ndim == 3:   # ravu: int11, int10, int01 passes
+            for i, pas in enumerate(("int11", "int10", "int01")):
+                f[pas] = _key_figures(k[i, :rows], {q: ref[q][i] for q in ("key", "boundary", "margin")})
+            f["note"] = ("int10/int01 keys read the GPU's FP16-stored int11, the oracle's its FP64 int11: "
+                         "their off-boundary flips come from that input difference")
+        else:
+            f.update(_key_figures(k[:rows], ref))
+        figs[f"config2 {n} {rows}x{W}->{2 * rows}x{2 * W} fp16 fast"] = f
+    for label, name, h, w, seed, fp16 in CHECKS:
+        ref = refs[label]
+        hm = models.get(name) or synth.model_for(name)[0]
+        x = torch.from_numpy(_frame(seed, h, w, fp16)).to(dev, torch.float16 if fp16 else torch.float32)
+        prec = "fast" if fp16 else "fp32"
+        if hm.family == "nnedi3":
+            y = hm.upscale(x, precision=prec)
+            f = _value_figures(y.float().cpu().numpy(), ref["out"])
+        else:
+            y, k = hm.upscale(x, precision=prec, return_keys=True)
+            f = _value_figures(y.float().cpu().numpy(), ref["out"])
+            f.update(_key_figures(k.cpu().numpy(), ref))
+        f["form"] = "fast (FP16 planes, FP16 tensor-core neurons)" if fp16 else "plain FP32"
+        figs[label] = f
+    figs["oracle"] = "FP64 NumPy restatement on the same inputs (outputs of the cpu_baseline leg)"
+    return figs
+
+
+def run_gpu(args, refs=None):
     import torch
     import torch.distributed as dist
     pkg = _pkg()
@@ -391,6 +506,9 @@ def run_gpu(args):
                        "batched_mpix_s": res["batched"], "batched_ratio": res["batched"] / res["fp32"],
                        "batched": f"{NFRAMES} FP16 frames per persistent launch, CUDA graph replay"}
 
+    # ---- precision of each configuration against the FP64 oracle
+    precision = precision_figures(models, refs, dev) if refs else None
+
     # ---- the other configurations, measured as batches (informational)
     configs = {}
     if args.configs:
@@ -431,7 +549,7 @@ def run_gpu(args):
         nm = models["nnedi3-nns128-win8x6"]
         res = {}
         for prec, dt in (("fast", torch.float16), ("fp32", torch.float32)):
-            xs = [torch.from_numpy(synth.luma_plane(720, 1280, 4200 + f)).to(dev, dt) for f in range(4)]
+            xs = [torch.from_numpy(synth.luma_plane(720, 1280, 3000 + f)).to(dev, dt) for f in range(4)]
             ys = [torch.empty((1440, 2560), dtype=dt, device=dev) for _ in range(4)]
             sc = torch.empty(2 * 720 * 1280 * xs[0].element_size(), dtype=torch.uint8, device=dev)
             run4 = lambda: [nm.run_raw([x], [y], out_size=(2560, 1440), precision=prec, scratch=sc)
@@ -515,6 +633,7 @@ def run_gpu(args):
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clocks,
         "headline": headline,
+        "precision": precision,
         "serving": serving,
         "other_configs": configs,
         "device": props.name,
@@ -645,10 +764,10 @@ def main():
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
-    cb = None
+    cb, refs = None, None
     if rank == 0 and world == 1 and not args.no_cpu:  # the CPU pool starts before any GPU call
-        cb = cpu_baseline(args.cpu_rows, len(os.sched_getaffinity(0)))
-    line = run_gpu(args)
+        cb, refs = cpu_baseline(args.cpu_rows, len(os.sched_getaffinity(0)), checks=True)
+    line = run_gpu(args, refs)
     if line is not None:
         line["cpu_baseline"] = cb
         print(json.dumps(line))

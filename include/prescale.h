@@ -131,6 +131,25 @@ typedef struct {
 int pz_version(void);
 const char* pz_last_error(void);
 
+/* ---- device-side errors ------------------------------------------------
+ * No counterpart in the reference (a shader cannot report an error to the
+ * mpv host).  Every device-side wait of the kernels (TMA copies, tensor-core
+ * MMA completion) is bounded in time; a wait that runs out abandons its
+ * tile and records the failure in a per-device error word instead of
+ * hanging the GPU.  pz_check_device_error waits for `cuda_stream`, reads
+ * and clears that word: PZ_OK, PZ_ETIMEDOUT (a bounded wait ran out; some
+ * output tiles of the launches since the last check were not written) or
+ * PZ_EIO (another device-side failure), with the message in
+ * pz_last_error().  The word is shared by every stream on the device. */
+int pz_check_device_error(void* cuda_stream);
+
+/* Test hook for the path above: enqueues on `cuda_stream` a kernel whose one
+ * CTA waits on an mbarrier that nothing arrives at (no copy, no MMA in
+ * flight), giving up after limit_ns nanoseconds and recording the timeout
+ * like a real kernel would; the next pz_check_device_error returns
+ * PZ_ETIMEDOUT. */
+int pz_selftest_wait(long long limit_ns, void* cuda_stream);
+
 int pz_model_create(const pz_model_desc* desc, pz_model** out);
 void pz_model_destroy(pz_model* model);
 
@@ -230,7 +249,9 @@ int pz_batch_run(const pz_job* jobs, int n_jobs, void* work, size_t work_bytes,
  * until the process exits.  The first call on each device looks up the
  * array's device address (cudaGetSymbolAddress); make that call before any
  * stream capture.  All calls share the array, so calls that overlap on the
- * GPU race on it: order them on one stream or with events. */
+ * GPU race on it: order them on one stream or with events.  opts->precision
+ * is checked as by pz_run; a device-side wait that runs out is reported by
+ * pz_check_device_error. */
 #define PZ_STATIC_SCRATCH_BYTES (16u * 1024u * 1024u)
 int pz_nnedi3_run_static(const pz_model* model, const pz_plane* in, pz_plane* out,
                          const pz_opts* opts, void* cuda_stream);

@@ -14,9 +14,9 @@ from .frame import Frame, plan_frame, prescale_frame, resample_plane  # noqa: F4
 from .models import Nnedi3Model, RavuModel, load_model  # noqa: F401
 from .prescaler import (PRECISIONS, HookModel, build_model_cache, cached_model, load_hook,  # noqa: F401
                         MODEL_DIR)
-from ._ffi import PrescaleError, PrescaleLibraryError  # noqa: F401
+from ._ffi import PrescaleError, PrescaleLibraryError, check_device  # noqa: F401
 
 __all__ = ["load_hook", "HookModel", "cached_model", "build_model_cache", "parse_hook_file",
            "format_hook", "model_to_hook", "write_hook",
            "Frame", "plan_frame", "prescale_frame", "resample_plane",
-           "HookParseError", "PrescaleError", "PrescaleLibraryError"]
+           "HookParseError", "PrescaleError", "PrescaleLibraryError", "check_device"]

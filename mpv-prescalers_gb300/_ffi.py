@@ -101,6 +101,8 @@ EXPORTS = {
                                    ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p]),
     "pz_resample": (ctypes.c_int, [ctypes.POINTER(Plane), ctypes.POINTER(Plane), ctypes.c_float, ctypes.c_float,
                                    ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_void_p]),
+    "pz_check_device_error": (ctypes.c_int, [ctypes.c_void_p]),
+    "pz_selftest_wait": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_void_p]),
 }
 
 # Size of the static intermediate-plane array behind pz_nnedi3_run_static.
@@ -134,3 +136,12 @@ def check(rc: int) -> None:
     if rc != PZ_OK:
         msg = lib().pz_last_error()
         raise PrescaleError(rc, msg.decode() if msg else "")
+
+
+def check_device(stream=None) -> None:
+    """Wait for `stream` (default: the current torch stream), read and clear
+    the device error word; raises :class:`PrescaleError` (code
+    ``PZ_ETIMEDOUT`` when a bounded device-side wait ran out)."""
+    import torch
+    s = torch.cuda.current_stream() if stream is None else stream
+    check(lib().pz_check_device_error(s.cuda_stream))

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../../include/prescale.h"
+#include "async.cuh"
 #include "kernels.h"
 #include "model.h"
 
@@ -41,10 +42,29 @@ int upload(T** dst, const void* src, size_t bytes) {
   return PZ_OK;
 }
 
+// The device-side error word every kernel reports into (first failure wins,
+// see kErr* in common.cuh).  A file-scope __device__ variable: nothing is
+// allocated for it, so the first launch on a device may come inside stream
+// capture.  Host code looks its device address up once per device.
+__device__ int g_device_err;
+
+constexpr int kMaxDevices = 64;
 std::mutex g_err_mu;
-std::vector<int*> g_err_words;  // per device
+int* g_err_words[kMaxDevices];  // device address of g_device_err, per device
 
 size_t dtype_size(int dt) { return dt == PZ_F32 ? 4 : 2; }
+
+// A bounded wait that nothing ever completes: the mbarrier is initialised for
+// one arrival and never arrived at, no copy or MMA is issued.  The wait gives
+// up after `limit_ns` and reports kErrWaitTimeout like every kernel does.
+__global__ void wait_selftest_kernel(int* err, unsigned long long limit_ns) {
+  __shared__ __align__(8) unsigned long long mbar;
+  const uint32_t mb = pz::smem_u32(&mbar);
+  if (threadIdx.x == 0) pz::mbar_init(mb, 1);
+  __syncthreads();
+  if (!__syncthreads_and(pz::mbar_wait_bounded(mb, 0u, limit_ns)) && threadIdx.x == 0)
+    atomicCAS(err, 0, pz::kErrWaitTimeout);
+}
 
 // `pairs`: the plane is written with 2-wide vector stores, so its base and
 // pitch must keep every even column 2-element aligned.
@@ -110,16 +130,22 @@ int set_error(int code, const char* fmt, ...) {
 
 int* device_error_word() {
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
   std::lock_guard<std::mutex> lk(g_err_mu);
-  if ((int)g_err_words.size() <= dev) g_err_words.resize(dev + 1, nullptr);
   if (!g_err_words[dev]) {
-    int* w = nullptr;
-    if (cudaMalloc(&w, sizeof(int)) != cudaSuccess) return nullptr;
-    if (cudaMemset(w, 0, sizeof(int)) != cudaSuccess) return nullptr;
-    g_err_words[dev] = w;
+    void* w = nullptr;
+    if (cudaGetSymbolAddress(&w, g_device_err) != cudaSuccess) return nullptr;
+    g_err_words[dev] = static_cast<int*>(w);
   }
   return g_err_words[dev];
+}
+
+int check_precision(const pz_opts* o, int dtype) {
+  if (o && (o->precision < PZ_PREC_FP32 || o->precision > PZ_PREC_MPV))
+    return set_error(PZ_EINVAL, "unknown precision %d", o->precision);
+  if (o && o->precision == PZ_PREC_MPV && dtype != PZ_F16)
+    return set_error(PZ_EINVAL, "the mpv form takes FP16 planes (the host's textures are rgba16f)");
+  return PZ_OK;
 }
 }  // namespace pz
 
@@ -387,10 +413,9 @@ int pz_run(const pz_model* m, const pz_plane* in, int n_in, pz_plane* out, int n
       return fail(PZ_EINVAL, "output planes differ in size");
   }
   const int W = in[0].width, H = in[0].height, dt = in[0].dtype;
-  if (o && (o->precision < PZ_PREC_FP32 || o->precision > PZ_PREC_MPV))
-    return fail(PZ_EINVAL, "unknown precision %d", o->precision);
-  if (o && o->precision == PZ_PREC_MPV && dt != PZ_F16)
-    return fail(PZ_EINVAL, "the mpv form takes FP16 planes (the host's textures are rgba16f)");
+  if ((rc = pz::check_precision(o, dt))) return rc;
+  int* err = pz::device_error_word();
+  if (!err) return fail(PZ_EIO, "device error word: cudaGetSymbolAddress failed");
   int OW = 2 * W, OH = 2 * H;
   if (m->family == PZ_RAVU_3X) {
     OW = 3 * W;
@@ -419,7 +444,7 @@ int pz_run(const pz_model* m, const pz_plane* in, int n_in, pz_plane* out, int n
     a.cs = m->d_cs;
     a.bias = m->d_bias;
     a.wts_h = m->d_wts_h;
-    a.err = pz::device_error_word();
+    a.err = err;
     void* tmp = nullptr;
     bool own_tmp = false;
     if (ax == 3) {
@@ -468,7 +493,7 @@ int pz_run(const pz_model* m, const pz_plane* in, int n_in, pz_plane* out, int n
     pz::select_lut(m, o ? o->precision : PZ_PREC_FP32, &a);
     a.ar = m->ar;
     a.keys = o ? o->keys : nullptr;
-    a.err = pz::device_error_word();
+    a.err = err;
     a.staging = o ? o->staging : 0;
     a.kp = m->kp;
     switch (m->family) {
@@ -480,6 +505,39 @@ int pz_run(const pz_model* m, const pz_plane* in, int n_in, pz_plane* out, int n
     }
     if (rc) return fail(rc, "no kernel for family %d radius %d", m->family, m->radius);
   }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+  return PZ_OK;
+}
+
+int pz_check_device_error(void* cuda_stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+  int* w = pz::device_error_word();
+  if (!w) return fail(PZ_EIO, "device error word: cudaGetSymbolAddress failed");
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+  int code = 0;
+  e = cudaMemcpy(&code, w, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "reading the device error word");
+  if (code == pz::kErrNone) return PZ_OK;
+  const int zero = 0;
+  e = cudaMemcpy(w, &zero, sizeof(int), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "clearing the device error word");
+  switch (code) {
+    case pz::kErrWaitTimeout:
+      return fail(PZ_ETIMEDOUT, "a bounded device-side wait ran out; the tiles of that launch were not written");
+    case pz::kErrTileOverflow:
+      return fail(PZ_EIO, "a ravu-zoom tile needed more input than its staging area (downscale?)");
+    default:
+      return fail(PZ_EIO, "device error code %d", code);
+  }
+}
+
+int pz_selftest_wait(long long limit_ns, void* cuda_stream) {
+  if (limit_ns < 0) return fail(PZ_EINVAL, "negative wait limit");
+  int* w = pz::device_error_word();
+  if (!w) return fail(PZ_EIO, "device error word: cudaGetSymbolAddress failed");
+  wait_selftest_kernel<<<1, 32, 0, static_cast<cudaStream_t>(cuda_stream)>>>(w, (unsigned long long)limit_ns);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
   return PZ_OK;

@@ -36,12 +36,13 @@ __device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity) {
   return ok != 0;
 }
 
-// Wait for phase `parity` of the mbarrier, giving up after kWaitNs.
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity) {
+// Wait for phase `parity` of the mbarrier, giving up after `limit_ns`.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity,
+                                                  unsigned long long limit_ns = kWaitNs) {
   if (mbar_try(mbar, parity)) return true;
   const unsigned long long t0 = globaltimer();
   while (!mbar_try(mbar, parity)) {
-    if (globaltimer() - t0 > kWaitNs) return false;
+    if (globaltimer() - t0 > limit_ns) return false;
   }
   return true;
 }

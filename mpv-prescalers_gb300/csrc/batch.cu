@@ -44,7 +44,6 @@ size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
 }  // namespace
 
-int* device_error_word();
 }  // namespace pz
 
 // Host plan: what one launch enqueues.
@@ -125,6 +124,7 @@ int build_tables(const pz_job* jobs, int n, std::vector<pz::DevJob>* table, pz_b
     a.ar = m->ar;
     a.keys = nullptr;
     a.err = pz::device_error_word();
+    if (!a.err) return pz::set_error(PZ_EIO, "device error word: cudaGetSymbolAddress failed");
     a.kp = m->kp;
     d.prog = en.prog;
     const bool zoom = m->family == PZ_RAVU_ZOOM;
@@ -167,10 +167,8 @@ int validate_job(const pz_job& j, int idx) {
         o.height != j.out[0].height)
       return pz::set_error(PZ_EINVAL, "job %d: planes differ in size", idx);
   }
-  if (j.opts.precision < PZ_PREC_FP32 || j.opts.precision > PZ_PREC_MPV)
-    return pz::set_error(PZ_EINVAL, "job %d: unknown precision %d", idx, j.opts.precision);
-  if (j.opts.precision == PZ_PREC_MPV && j.in[0].dtype != PZ_F16)
-    return pz::set_error(PZ_EINVAL, "job %d: the mpv form takes FP16 planes", idx);
+  int rc;
+  if ((rc = pz::check_precision(&j.opts, j.in[0].dtype))) return rc;
   const int W = j.in[0].width, H = j.in[0].height, OW = j.out[0].width, OH = j.out[0].height;
   const size_t es = j.in[0].dtype == PZ_F32 ? 4 : 2;
   switch (m->family) {

@@ -29,6 +29,15 @@ namespace pz {
 // Record `msg` for pz_last_error() on the calling thread; returns `code`.
 int set_error(int code, const char* fmt, ...);
 
+// Device address of the error word the kernels report into (one per device,
+// a __device__ variable: nothing is allocated); null if the lookup failed.
+// pz_check_device_error reads and clears it.
+int* device_error_word();
+
+// pz_run's checks of opts->precision against the plane dtype (PZ_OK or
+// PZ_EINVAL with the message set).
+int check_precision(const pz_opts* o, int dtype);
+
 // Does the fast form read this model's LUT as FP16 texels?  The lite, 3x and
 // zoom programs gather a whole LUT row (or four bilinear texels per block)
 // per pixel and are bound by those L1 gathers; FP16 halves them.  The ravu

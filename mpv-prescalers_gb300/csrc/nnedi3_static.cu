@@ -18,10 +18,11 @@
 // current, and later calls reuse it.  Make that first call before any stream
 // capture.  All calls share the one array and it keeps whatever the last
 // call left in it: nothing in it has to start at zero (the row pass writes
-// the whole intermediate before the column pass reads it), and the
-// device-side error word is cleared at the start of every call.  Calls that
-// overlap on the GPU (several streams, or several threads without ordering
-// between them) race on the array; order them.
+// the whole intermediate before the column pass reads it).  A bounded
+// device-side wait that runs out is reported in the library's device error
+// word (a __device__ variable as well), which pz_check_device_error reads and
+// clears.  Calls that overlap on the GPU (several streams, or several threads
+// without ordering between them) race on the array; order them.
 #include <cstring>
 #include <mutex>
 
@@ -32,7 +33,6 @@
 namespace {
 
 __device__ __align__(256) unsigned char g_static_scratch[PZ_STATIC_SCRATCH_BYTES];
-__device__ int g_static_err;
 
 constexpr int kMaxDevices = 64;
 struct StaticAddr {
@@ -42,7 +42,8 @@ struct StaticAddr {
 std::mutex g_addr_mu;
 StaticAddr g_addr[kMaxDevices];  // resolved on the first call on each device
 
-// Device addresses of the static array and error word on the current device.
+// Device addresses of the static array and of the error word on the current
+// device.
 int resolve_static(StaticAddr* out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -51,13 +52,12 @@ int resolve_static(StaticAddr* out) {
   std::lock_guard<std::mutex> lk(g_addr_mu);
   if (!g_addr[dev].scratch) {
     void* s = nullptr;
-    void* w = nullptr;
     e = cudaGetSymbolAddress(&s, g_static_scratch);
     if (e != cudaSuccess) return pz::set_error(PZ_EIO, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
-    e = cudaGetSymbolAddress(&w, g_static_err);
-    if (e != cudaSuccess) return pz::set_error(PZ_EIO, "cudaGetSymbolAddress(error word): %s", cudaGetErrorString(e));
+    int* w = pz::device_error_word();
+    if (!w) return pz::set_error(PZ_EIO, "device error word: cudaGetSymbolAddress failed");
     g_addr[dev].scratch = s;
-    g_addr[dev].err = static_cast<int*>(w);
+    g_addr[dev].err = w;
   }
   *out = g_addr[dev];
   return PZ_OK;
@@ -85,6 +85,7 @@ extern "C" int pz_nnedi3_run_static(const pz_model* m, const pz_plane* in, pz_pl
   int rc;
   if ((rc = check(in, "in", false)) || (rc = check(out, "out", (ax & 2) != 0))) return rc;
   if (out->dtype != in->dtype) return pz::set_error(PZ_EINVAL, "in and out must share one dtype");
+  if ((rc = pz::check_precision(o, in->dtype))) return rc;
   const int W = in->width, H = in->height, dt = in->dtype;
   const size_t es = dt == PZ_F32 ? 4 : 2;
   const int OW = (ax & 2) ? 2 * W : W, OH = (ax & 1) ? 2 * H : H;
@@ -99,8 +100,6 @@ extern "C" int pz_nnedi3_run_static(const pz_model* m, const pz_plane* in, pz_pl
   StaticAddr addr;
   if ((rc = resolve_static(&addr))) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  cudaError_t e = cudaMemsetAsync(addr.err, 0, sizeof(int), s);
-  if (e != cudaSuccess) return pz::set_error(PZ_EIO, "clearing the error word: %s", cudaGetErrorString(e));
 
   const bool fast = o && o->precision == PZ_PREC_FAST && pz::nnedi3_tc_supported(m->nns, m->win_h);
   pz::NnArgs a{};
@@ -129,7 +128,7 @@ extern "C" int pz_nnedi3_run_static(const pz_model* m, const pz_plane* in, pz_pl
     rc = pass(true, in->data, W, H, in->pitch, out->data, out->pitch);
   }
   if (rc) return pz::set_error(rc, "NNEDI3 launch configuration not supported");
-  e = cudaGetLastError();
+  const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return pz::set_error(PZ_EIO, "kernel launch: %s", cudaGetErrorString(e));
   return PZ_OK;
 }

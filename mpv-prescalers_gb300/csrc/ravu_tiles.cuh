@@ -124,6 +124,15 @@ __device__ int stage_planes_tma(const RavuArgs& p, TmaCtx* t, int x0, int y0, fl
   return 1;
 }
 
+// A CTA whose TMA wait timed out may still have that copy in flight into its
+// landing area: before the CTA exits, thread 0 waits (bounded again) for the
+// outstanding phase, so the copy never lands in shared memory that another
+// CTA owns.  Nothing else touches the landing area or the mbarrier once the
+// CTA is marked dead.
+__device__ __forceinline__ void tma_drain(const TmaCtx* t) {
+  if (t && t->dead && threadIdx.x == 0) (void)mbar_wait_bounded(t->mbar, t->phase);
+}
+
 // Stage the frame tile by TMA when possible, else by clamped loads.
 // Returns false only when a TMA wait timed out (the tile is abandoned).
 template <int CM, int TW, int TH, typename T>
@@ -722,6 +731,7 @@ __device__ __forceinline__ void tile_body(const RavuArgs& p, const TmaMaps& maps
     TmaCtx ctx{maps.map, smem_u32(&mbar),
                reinterpret_cast<unsigned char*>(tile_smem) + ((Prog::smem_bytes + 127) & ~(size_t)127), 0u, 0};
     Prog::run(p, blockIdx.x * kTileW, blockIdx.y * kTileH, smem, &ctx);
+    tma_drain(&ctx);
   } else {
     Prog::run(p, blockIdx.x * kTileW, blockIdx.y * kTileH, smem, nullptr);
   }
@@ -865,6 +875,7 @@ __device__ __forceinline__ void persistent_body(const DevJob* __restrict__ jobs,
     // when done with this tile.
     Prog::run(s_args, (t % tw) * kTileW, (t / tw) * kTileH, smem, Prog::kPlanes > 0 ? &ctx : nullptr);
   }
+  tma_drain(&ctx);
 }
 
 template <class Prog>

@@ -140,26 +140,52 @@ def structure_key(lum: List[np.ndarray], model) -> Dict[str, np.ndarray]:
         coherence = np.where(mu >= c1, 2.0, np.where(mu >= c0, 1.0, 0.0))
         key = ((angle * nstr + strength) * 3.0 + coherence).astype(np.int64)   # raw, may reach rows
 
-        # ---- boundary detection: FP32 rounding bound on each threshold test
-        E = FP32_BUDGET * T + 1e-30
+        margin = key_margin(a, b, d, T, L1, L2, theta, lam, mu, ssum, q if kind == "log2" else None, model)
+        bnd = margin <= FP32_BUDGET
+    return {"key": key, "boundary": bnd, "margin": margin, "theta": theta, "lambda": lam, "mu": mu,
+            "rows": 24 * nstr * 3}
+
+
+def key_margin(a, b, d, T, L1, L2, theta, lam, mu, ssum, q, model) -> np.ndarray:
+    """Distance of a key from its nearest quantisation decision, in units of
+    a relative error budget B of the structure tensor.
+
+    An FP32 evaluation perturbs (a, b, d) by about B * T (T = a + d, the
+    tensor's scale) with B a small multiple of 2^-24; each threshold test
+    moves by that perturbation times its first-order sensitivity (angle:
+    2 E / |(L1 - a, b)|; lambda: E / (2 lambda); log2 strength:
+    E / (2 L1 ln 2) + B; coherence: E / |L2| + E / L1; the eps gates: E).
+    The margin is, over all tests of the key, the smallest B at which the
+    test's threshold lies within reach; a key is a *boundary* key when its
+    margin is at most FP32_BUDGET.  A flat window (T = 0) is exact in any
+    precision: margin +inf.
+    """
+    inf = np.inf
+    with np.errstate(invalid="ignore", divide="ignore"):
+        Ts = np.maximum(T, 1e-300)
+
+        def m_of(dist, sens, const=0.0):
+            m = (np.abs(dist) - const) / sens
+            return np.where(np.isfinite(m), np.maximum(m, 0.0), inf)
+
         r = np.hypot(L1 - a, b)
-        dtheta = 2.0 * E / np.maximum(r, 1e-300)
         qa = theta * 24.0 / PI
-        bnd = np.abs(qa - np.round(qa)) <= (24.0 / PI) * dtheta + 1e-9
-        bnd |= np.abs(np.abs(b) - FLT_EPS) <= E
+        m = m_of(qa - np.round(qa), (24.0 / PI) * 2.0 * Ts / np.maximum(r, 1e-300), 1e-9)
+        m = np.minimum(m, m_of(np.abs(b) - FLT_EPS, Ts))
+        kind = model.strength[0]
         if kind == "log2":
-            dq = (E / np.maximum(2.0 * L1, 1e-300)) / math.log(2.0) + FP32_BUDGET
-            bnd |= (np.abs(q - np.round(q)) <= dq) & (q > -0.5) & (q < model.strength[2] + 0.5)
+            sens = (Ts / np.maximum(2.0 * L1, 1e-300)) / math.log(2.0) + 1.0
+            inrange = (q > -0.5) & (q < model.strength[2] + 0.5)
+            m = np.minimum(m, np.where(inrange, m_of(q - np.round(q), sens), inf))
         else:
             for t in model.strength[1]:
-                bnd |= np.abs(lam - t) <= E / (2.0 * t) + FP32_BUDGET * t
-        bnd |= np.abs(L2) <= E
-        dmu = E / np.maximum(np.abs(L2), 1e-300) + E / np.maximum(L1, 1e-300)
-        for c in (c0, c1):
-            bnd |= np.abs(mu - c) <= dmu + 1e-9
-        bnd |= np.abs(ssum * ssum - FLT_EPS * FLT_EPS) <= 2.0 * E
-        bnd &= T > 0.0        # a flat window is exact in any precision
-    return {"key": key, "boundary": bnd, "theta": theta, "lambda": lam, "mu": mu, "rows": 24 * nstr * 3}
+                m = np.minimum(m, m_of(lam - t, Ts / (2.0 * t) + t))
+        m = np.minimum(m, m_of(L2, Ts))
+        sens_mu = Ts / np.maximum(np.abs(L2), 1e-300) + Ts / np.maximum(L1, 1e-300)
+        for c in model.coherence:
+            m = np.minimum(m, m_of(mu - c, sens_mu, 1e-9))
+        m = np.minimum(m, m_of(ssum * ssum - FLT_EPS * FLT_EPS, 2.0 * Ts))
+        return np.where(T > 0.0, m, inf)
 
 
 def _row(key: np.ndarray, rows: int) -> np.ndarray:
@@ -355,6 +381,7 @@ def ravu_lattice(model, planes, keys: Optional[np.ndarray] = None, int11: Option
         src11 = np.asarray(int11, dtype=np.float64).reshape(C, H, W)
     out_keys = [i11["key"]]
     bnd = [i11["boundary"]]
+    margins = [i11["margin"]]
     results = {}
     for li, lattice in ((1, "int10"), (2, "int01")):
         vals = []
@@ -364,12 +391,13 @@ def ravu_lattice(model, planes, keys: Optional[np.ndarray] = None, int11: Option
         results[lattice], inf = _ravu_pass(model, vals, None if kf is None else kf[li])
         out_keys.append(inf["key"])
         bnd.append(inf["boundary"])
+        margins.append(inf["margin"])
     out = np.empty((C, 2 * H, 2 * W))
     out[:, 0::2, 0::2] = x
     out[:, 0::2, 1::2] = results["int10"]
     out[:, 1::2, 0::2] = results["int01"]
     out[:, 1::2, 1::2] = own11
-    return out, {"key": np.stack(out_keys), "boundary": np.stack(bnd)}
+    return out, {"key": np.stack(out_keys), "boundary": np.stack(bnd), "margin": np.stack(margins)}
 
 
 # ----------------------------------------------------------- ravu-zoom ----

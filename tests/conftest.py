@@ -28,11 +28,34 @@ def _load_package():
 
 _load_package()
 
-REFERENCE = os.environ.get("PRESCALER_REFERENCE", "/root/reference")
+# the reference checkout: $PRESCALER_REFERENCE, else a sibling directory
+# named "reference" next to this repository
+REFERENCE = os.environ.get("PRESCALER_REFERENCE", os.path.join(os.path.dirname(REPO), "reference"))
 
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+@pytest.fixture(autouse=True)
+def _no_silent_device_errors(request):
+    """After every GPU test: no bounded device-side wait ran out unnoticed
+    (the kernels record that in the device error word instead of hanging)."""
+    yield
+    if request.node.get_closest_marker("gpu") is None:
+        return
+    try:
+        import torch
+    except ImportError:
+        return
+    if not torch.cuda.is_available():
+        return
+    from mpv_prescalers_gb300 import _ffi
+    if _ffi._lib is None:   # the test never loaded the library
+        return
+    lib = _ffi.lib()
+    rc = lib.pz_check_device_error(torch.cuda.current_stream().cuda_stream)
+    assert rc == _ffi.PZ_OK, f"device error after the test: {lib.pz_last_error().decode()}"
 
 
 @pytest.fixture(scope="session")

@@ -34,9 +34,10 @@ def _plane(t):
     return _ffi.Plane(t.data_ptr(), t.shape[1], t.shape[0], t.stride(0), dt)
 
 
-def _run_static(hm, x, out, axes=0):
+def _run_static(hm, x, out, axes=0, precision="fp32"):
     o = _ffi.Opts()
     o.nnedi3_axes = axes
+    o.precision = {"fp32": _ffi.PZ_PREC_FP32, "fast": _ffi.PZ_PREC_FAST, "mpv": _ffi.PZ_PREC_MPV}[precision]
     pin, pout = _plane(x), _plane(out)
     lib = _ffi.lib()
     rc = lib.pz_nnedi3_run_static(hm.device_handle(x.device.index), ctypes.byref(pin), ctypes.byref(pout),
@@ -56,6 +57,39 @@ def test_static_entry_matches_pz_run_on_two_calls_in_a_row(dtype):
         torch.cuda.synchronize()
         assert torch.isfinite(out).all()
         assert (out.float() - ref.float()).abs().max().item() <= TOL
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float16])
+def test_static_entry_fast_form_matches_pz_run_on_two_calls_in_a_row(dtype):
+    """The tensor-core form: its column pass reads the row-doubled plane
+    from the static array at pitch W; compared with pz_run in the same form
+    (FP16 tensor-core neurons), which the parity tests compare with the
+    oracle.  The tolerance is the fast form's (2e-3): both calls run the same
+    kernels on the same input, so in practice they agree exactly."""
+    hm, _ = synth.model_for("nnedi3-nns128-win8x6")
+    for seed in (3, 4):
+        x = torch.from_numpy(synth.luma_plane(180, 320, seed)).to("cuda", dtype)
+        ref = hm.upscale(x, precision="fast")
+        out = torch.full_like(ref, float("nan"))
+        rc, msg = _run_static(hm, x, out, precision="fast")
+        assert rc == 0, msg
+        torch.cuda.synchronize()
+        assert torch.isfinite(out).all()
+        assert (out.float() - ref.float()).abs().max().item() <= 2e-3
+
+
+def test_precision_is_checked_like_pz_run():
+    hm, _ = synth.model_for("nnedi3-nns16-win8x4")
+    x = torch.zeros((20, 30), device="cuda")
+    out = torch.empty((40, 60), device="cuda")
+    o = _ffi.Opts()
+    o.precision = 7
+    lib = _ffi.lib()
+    rc = lib.pz_nnedi3_run_static(hm.device_handle(0), ctypes.byref(_plane(x)), ctypes.byref(_plane(out)),
+                                  ctypes.byref(o), torch.cuda.current_stream().cuda_stream)
+    assert rc == _ffi.PZ_EINVAL and b"precision" in lib.pz_last_error()
+    rc, msg = _run_static(hm, x, out, precision="mpv")   # the mpv form takes FP16 planes only
+    assert rc == _ffi.PZ_EINVAL and "FP16" in msg
 
 
 def test_largest_fp32_frame_that_fits_and_single_axis():
