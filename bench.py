@@ -314,12 +314,28 @@ def _key_figures(kg, ref):
             "max_mismatch_margin_ulp": float(marg.max()) if marg.size else 0.0}
 
 
-def _value_figures(y, ref_out):
-    """max-abs and PSNR (peak 1.0) of GPU output rows against the oracle's."""
+def _value_figures(y, ref_out, flipped=None):
+    """max-abs and PSNR (peak 1.0) of GPU output rows against the oracle's;
+    with `flipped` (output pixels whose own LUT key differs from the
+    oracle's) also the max-abs over the pixels whose keys agree."""
     y = np.asarray(y, dtype=np.float64).reshape(ref_out.shape)
-    d = y - ref_out.astype(np.float64)
+    d = np.abs(y - ref_out.astype(np.float64))
     mse = float(np.mean(d * d))
-    return {"max_abs": float(np.abs(d).max()), "psnr_db": float("inf") if mse == 0 else 10 * np.log10(1 / mse)}
+    f = {"max_abs": float(d.max()), "psnr_db": float("inf") if mse == 0 else 10 * np.log10(1 / mse)}
+    if flipped is not None:
+        keep = ~flipped
+        f["max_abs_key_matched"] = float(d[..., keep].max()) if keep.any() else 0.0
+    return f
+
+
+def _flipped(family, mism, out_hw):
+    """Output pixels of flipped keys: the 2x2 block of a lite key, the lattice
+    sample of an int11 / int10 / int01 key."""
+    if family == "ravu":
+        m = np.zeros(out_hw, dtype=bool)
+        m[1::2, 1::2], m[0::2, 1::2], m[1::2, 0::2] = mism[0], mism[1], mism[2]
+        return m
+    return np.repeat(np.repeat(mism, 2, 0), 2, 1)
 
 
 def precision_figures(models, refs, dev):
@@ -333,8 +349,10 @@ def precision_figures(models, refs, dev):
         rows = ref["out"].shape[-2] // 2
         x = torch.from_numpy(_frame(SEED0)).to(dev, torch.float16)
         y, k = models[n].upscale(x, precision="fast", return_keys=True)
-        f = _value_figures(y.float().cpu().numpy()[..., :2 * rows, :], ref["out"])
         k = k.cpu().numpy()
+        mism = k[..., :rows, :] != ref["key"]
+        f = _value_figures(y.float().cpu().numpy()[..., :2 * rows, :], ref["out"],
+                           _flipped(models[n].family, mism, ref["out"].shape[-2:]))
         if k.ndim == 3:   # ravu: int11, int10, int01 passes
             for i, pas in enumerate(("int11", "int10", "int01")):
                 f[pas] = _key_figures(k[i, :rows], {q: ref[q][i] for q in ("key", "boundary", "margin")})
@@ -353,8 +371,10 @@ def precision_figures(models, refs, dev):
             f = _value_figures(y.float().cpu().numpy(), ref["out"])
         else:
             y, k = hm.upscale(x, precision=prec, return_keys=True)
-            f = _value_figures(y.float().cpu().numpy(), ref["out"])
-            f.update(_key_figures(k.cpu().numpy(), ref))
+            k = k.cpu().numpy()
+            f = _value_figures(y.float().cpu().numpy(), ref["out"],
+                               _flipped(hm.family, k.reshape(ref["key"].shape) != ref["key"], ref["out"].shape[-2:]))
+            f.update(_key_figures(k, ref))
         f["form"] = "fast (FP16 planes, FP16 tensor-core neurons)" if fp16 else "plain FP32"
         figs[label] = f
     figs["oracle"] = "FP64 NumPy restatement on the same inputs (outputs of the cpu_baseline leg)"

@@ -194,14 +194,14 @@ int pz_model_create(const pz_model_desc* d, pz_model** out) {
       bias[2 * k + 1] = d->bias_b[k];
     }
     // tensor-core operand B [2*nns][KP] FP16, chunk-major: chunk c of NC
-    // neurons (NC = 32, or 16 for nns16) is NC softmax-branch rows followed by
+    // neurons (NC = min(32, nns / 2)) is NC softmax-branch rows followed by
     // NC Elliott-branch rows.  Row = [weights (T taps), sum of the weights,
     // bias hi, bias lo, 0...]; against A rows [x_hat, mean*invstd, 1, 1, 0...]
     // the MMA yields the whole pre-activation <x,w>*invstd + b.  Softmax rows
     // are scaled by log2(e) so the epilogue takes exp2 directly.  Stored as
     // no-swizzle K-major core matrices (8 rows x 8 halves; K-neighbours 64
     // halves apart, 8-row groups 8*KP apart).
-    const int NC = n < 32 ? n : 32;
+    const int NC = pz::nnedi3_tc_chunk(n);
     const double kLog2e = 1.4426950408889634;
     for (int r = 0; r < 2 * n; r++) {
       const int chunk = r / (2 * NC), within = r % (2 * NC);

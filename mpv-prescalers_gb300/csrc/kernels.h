@@ -53,5 +53,8 @@ int launch_zoom(const RavuArgs& a, int radius, int chmode, bool ar, int dtype, c
 int launch_nnedi3_simt(const NnArgs& a, bool xpass, int dtype, cudaStream_t s);
 int launch_nnedi3_tc(const NnArgs& a, bool xpass, int dtype, cudaStream_t s);
 bool nnedi3_tc_supported(int nns, int win_h);
+// Neurons per group of the tensor-core weight operand: the host stores B
+// chunk-major, NC softmax rows then NC Elliott rows per group.
+int nnedi3_tc_chunk(int nns);
 
 }  // namespace pz

@@ -1,7 +1,9 @@
-"""Recipe: compile the reference's own root ``.hook`` shader text as C++.
+"""Recipe: compile the reference's own ``.hook`` shader text as C++.
 
-Test infrastructure.  For each root ``.hook`` file of the reference (read in
-place, never copied into the repository) this script
+Test infrastructure.  For each ``.hook`` file of the reference named on the
+command line -- root fragment-shader files, or ``compute/<name>`` for the
+compute-shader form (the only form of ravu-3x) -- read in place, never copied
+into the repository, this script
 
 1. splits the file into pass blocks and texture blocks,
 2. rewrites the two GLSL swizzles C++ cannot express as members
@@ -17,7 +19,13 @@ place, never copied into the repository) this script
    which runs every enabled pass of the file in order, exactly like the mpv
    hook host would (clamp-to-edge textures, per-pixel ``hook()`` calls,
    ``//!SAVE`` / hooked-texture replacement, ``//!WIDTH``/``//!HEIGHT``/
-   ``//!WHEN`` evaluated as RPN).
+   ``//!WHEN`` evaluated as RPN).  A ``//!COMPUTE bw bh tw th`` pass is
+   dispatched over ceil(W / bw) x ceil(H / bh) workgroups of tw x th
+   invocations; each workgroup runs its invocations serially in phases
+   split at ``barrier()`` (``glsl_shim.hpp``, ``Compute``), ``shared``
+   arrays are static, ``imageStore`` writes the pass's output texture.
+
+The library of ``compute/<name>.hook`` is ``oracle/_ref/compute.<name>.so``.
 
 Outputs go only to ``oracle/_ref/`` (git-ignored).  Usage::
 
@@ -40,6 +48,29 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 DEFAULT_REF = "/root/reference"
+
+COMPUTE_DECLS = r"""
+static Compute C;
+#define gl_WorkGroupID (C.wg_id)
+#define gl_LocalInvocationID (C.local_id)
+#define gl_GlobalInvocationID (C.global_id)
+#define gl_WorkGroupSize (C.wg_size)
+#define gl_LocalInvocationIndex (C.local_index)
+#define barrier() do { if (++C.bar > C.phase) return; } while (0)
+#define shared static
+static const int out_image = 0;
+inline void imageStore(int, const ivec2& p, const vec4& v) { C.store(p.x, p.y, v); }
+// output pixel id -> normalised input position, texel centres aligned
+inline vec2 HOOKED_map(const ivec2& id) { return vec2((id.x + 0.5) / C.out->w, (id.y + 0.5) / C.out->h); }
+"""
+COMPUTE_MACROS = ["gl_WorkGroupID", "gl_LocalInvocationID", "gl_GlobalInvocationID", "gl_WorkGroupSize",
+                  "gl_LocalInvocationIndex", "barrier", "shared"]
+
+
+def out_stem(stem: str) -> str:
+    """File stem under oracle/_ref of a reference path stem ("compute/x" -> "compute.x")."""
+    return stem.replace("/", ".")
+
 
 RPN_CPP = r"""
 #include "glsl_shim.hpp"
@@ -123,11 +154,15 @@ def gen_cpp(stem: str, passes, textures) -> str:
         o.append("static Frag F;")
         o.append("using glsl::mix; using glsl::clamp; using glsl::max; using glsl::min; using glsl::floor;"
                  " using glsl::fract; using glsl::mod; using glsl::atan; using glsl::sqrt; using glsl::inversesqrt;"
-                 " using glsl::log2; using glsl::exp; using glsl::abs; using glsl::dot; using glsl::matrixCompMult;")
+                 " using glsl::log2; using glsl::exp; using glsl::abs; using glsl::dot; using glsl::matrixCompMult;"
+                 " using glsl::outerProduct;")
         o.append("#define HOOKED_pos (F.pos)")
         o.append("#define HOOKED_size (F.size)")
         o.append("#define HOOKED_pt (vec2(1.0 / F.size.x, 1.0 / F.size.y))")
         o.append("inline vec4 texture(const Tex* t, const vec2& uv) { return t->sample(uv); }")
+        compute = "COMPUTE" in p["dirs"]
+        if compute:
+            o.append(COMPUTE_DECLS)
         for b in p["dirs"]["BIND"]:
             if b in tex_names:
                 o.append(f"static const Tex* {b} = nullptr;")
@@ -135,8 +170,12 @@ def gen_cpp(stem: str, passes, textures) -> str:
                 o.append(f"static const Tex* t_{b} = nullptr;")
                 o.append(f"inline vec4 {b}_texOff(const vec2& off) {{ return tex_off(*t_{b}, F, off); }}")
                 o.append(f"inline vec4 {b}_tex(const vec2& uv) {{ return t_{b}->sample(uv); }}")
+                if b != "HOOKED":
+                    o.append(f"#define {b}_pt (vec2(1.0 / t_{b}->w, 1.0 / t_{b}->h))")
+                    o.append(f"#define {b}_size (vec2(t_{b}->w, t_{b}->h))")
+                    macros = macros + [f"{b}_pt", f"{b}_size"]
         o.append(body)
-        for m in macros + ["HOOKED_pos", "HOOKED_size", "HOOKED_pt"]:
+        for m in macros + ["HOOKED_pos", "HOOKED_size", "HOOKED_pt"] + (COMPUTE_MACROS if compute else []):
             o.append(f"#undef {m}")
         o.append(f"}}  // namespace p{k}")
     o.append("#undef float")
@@ -153,7 +192,7 @@ def gen_cpp(stem: str, passes, textures) -> str:
     o.append("  static bool loaded = false;")
     o.append("  if (!loaded) {")
     for t in textures:
-        fn = os.path.join(OUT, f"{stem}__{t['name']}.hex")
+        fn = os.path.join(OUT, f"{out_stem(stem)}__{t['name']}.hex")
         o.append(f'    load_lut("{t["name"]}", "{fn}", {t["w"]}, {t["h"]}, {"true" if t["filter"] == "LINEAR" else "false"});')
     o.append("    loaded = true; }")
     o.append("  Tex hooked; hooked.w = W; hooked.h = H; hooked.px.resize((size_t)W * H);")
@@ -166,6 +205,7 @@ def gen_cpp(stem: str, passes, textures) -> str:
         when = d.get("WHEN")
         cond = f'rpn("{when}", env) != 0.0' if when else "true"
         o.append(f"    if ({cond}) {{")
+        o.append("      (void)env;")
         wexpr = f'(int)rpn("{d["WIDTH"]}", env)' if "WIDTH" in d else "hooked.w"
         hexpr = f'(int)rpn("{d["HEIGHT"]}", env)' if "HEIGHT" in d else "hooked.h"
         o.append(f"      int ow = {wexpr}, oh = {hexpr};")
@@ -178,10 +218,26 @@ def gen_cpp(stem: str, passes, textures) -> str:
             else:
                 o.append(f'      p{k}::t_{b} = &saved["{b}"];')
         o.append(f"      p{k}::F.size = vec2(hooked.w, hooked.h);")
-        o.append("      for (int y = 0; y < oh; y++) for (int x = 0; x < ow; x++) {")
-        o.append(f"        p{k}::F.pos = vec2((x + 0.5) / ow, (y + 0.5) / oh);")
-        o.append(f"        res.px[(size_t)y * ow + x] = p{k}::hook();")
-        o.append("      }")
+        if "COMPUTE" in d:
+            cw = [int(v) for v in d["COMPUTE"].split()]
+            bw, bh = cw[0], cw[1]
+            tw, th = (cw[2], cw[3]) if len(cw) >= 4 else (bw, bh)
+            nbar = len(re.findall(r"\bbarrier\s*\(\s*\)", "\n".join(p["body"])))
+            o.append(f"      p{k}::C.out = &res;")
+            o.append(f"      p{k}::C.wg_size.x = {tw}; p{k}::C.wg_size.y = {th}; p{k}::C.wg_size.z = 1;")
+            o.append(f"      for (int wy = 0; wy < (oh + {bh - 1}) / {bh}; wy++) for (int wx = 0; wx < (ow + {bw - 1}) / {bw}; wx++)")
+            o.append(f"        for (int ph = 0; ph <= {nbar}; ph++) for (int ly = 0; ly < {th}; ly++) for (int lx = 0; lx < {tw}; lx++) {{")
+            o.append(f"          Compute& c = p{k}::C;")
+            o.append("          c.wg_id.x = wx; c.wg_id.y = wy; c.local_id.x = lx; c.local_id.y = ly;")
+            o.append(f"          c.global_id.x = wx * {tw} + lx; c.global_id.y = wy * {th} + ly;")
+            o.append(f"          c.local_index = ly * {tw} + lx; c.bar = 0; c.phase = ph;")
+            o.append(f"          p{k}::hook();")
+            o.append("        }")
+        else:
+            o.append("      for (int y = 0; y < oh; y++) for (int x = 0; x < ow; x++) {")
+            o.append(f"        p{k}::F.pos = vec2((x + 0.5) / ow, (y + 0.5) / oh);")
+            o.append(f"        res.px[(size_t)y * ow + x] = p{k}::hook();")
+            o.append("      }")
         if d.get("SAVE"):
             o.append(f'      saved["{d["SAVE"]}"] = res;')
         else:
@@ -202,12 +258,12 @@ def build_one(ref: str, stem: str) -> str:
         text = f.read()
     passes, textures = split_blocks(text)
     for t in textures:
-        with open(os.path.join(OUT, f"{stem}__{t['name']}.hex"), "w") as f:
+        with open(os.path.join(OUT, f"{out_stem(stem)}__{t['name']}.hex"), "w") as f:
             f.write(t["hex"])
-    cpp = os.path.join(OUT, stem + ".cpp")
+    cpp = os.path.join(OUT, out_stem(stem) + ".cpp")
     with open(cpp, "w") as f:
         f.write(gen_cpp(stem, passes, textures))
-    so = os.path.join(OUT, stem + ".so")
+    so = os.path.join(OUT, out_stem(stem) + ".so")
     cmd = ["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fPIC", "-shared", "-w",
            f"-I{HERE}", "-o", so, cpp, os.path.join(OUT, "rpn.o")]
     subprocess.run(cmd, check=True)
@@ -232,7 +288,7 @@ def compile_generated(names) -> list:
         return []
     todo = []
     for stem in names:
-        cpp, so = os.path.join(OUT, stem + ".cpp"), os.path.join(OUT, stem + ".so")
+        cpp, so = os.path.join(OUT, out_stem(stem) + ".cpp"), os.path.join(OUT, out_stem(stem) + ".so")
         if os.path.exists(cpp) and (stale(cpp, so) or not loads(so)):
             todo.append((cpp, so))
     if not todo:

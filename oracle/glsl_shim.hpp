@@ -1,6 +1,11 @@
-// GLSL-subset shim that lets the reference's fragment-shader bodies compile
-// as C++ (evaluated in double precision).  Test infrastructure: used only by
-// oracle/build_ref.py to run the reference's own shader text on the CPU.
+// GLSL-subset shim that lets the reference's fragment- and compute-shader
+// bodies compile as C++ (evaluated in double precision).  Test
+// infrastructure: used only by oracle/build_ref.py to run the reference's own
+// shader text on the CPU.
+//
+// Compute passes (//!COMPUTE) get uvec3 / ivec2, the gl_* invocation ids,
+// `shared` arrays, barrier() and imageStore (see `Compute` below); the
+// recipe runs each workgroup's invocations one after another in phases.
 //
 // Covers what the root .hook files use: vec2/vec3/vec4 with .x .y .z .w
 // members plus .xyz() / .wzyx() (the recipe rewrites those two swizzles
@@ -25,6 +30,25 @@ struct vec2;
 struct vec3;
 struct vec4;
 
+// integer vectors of the compute passes
+struct uvec3 {
+  unsigned x = 0, y = 0, z = 0;
+};
+struct ivec2 {
+  int x, y;
+  ivec2() : x(0), y(0) {}
+  explicit ivec2(int s) : x(s), y(s) {}
+  ivec2(int a, int b) : x(a), y(b) {}
+  explicit ivec2(const uvec3& u) : x((int)u.x), y((int)u.y) {}
+  explicit ivec2(const vec2& v);  // truncation, as GLSL's int()
+};
+inline ivec2 operator*(const ivec2& a, const ivec2& b) { return ivec2(a.x * b.x, a.y * b.y); }
+inline ivec2 operator*(const ivec2& a, int s) { return ivec2(a.x * s, a.y * s); }
+inline ivec2 operator+(const ivec2& a, const ivec2& b) { return ivec2(a.x + b.x, a.y + b.y); }
+inline ivec2 operator-(const ivec2& a, const ivec2& b) { return ivec2(a.x - b.x, a.y - b.y); }
+inline ivec2 operator+(const ivec2& a, int s) { return ivec2(a.x + s, a.y + s); }
+inline ivec2 operator-(const ivec2& a, int s) { return ivec2(a.x - s, a.y - s); }
+
 #define GLSL_VEC_OPS(V, N)                                                       \
   real& operator[](int i) { return (&x)[i]; }                                    \
   real operator[](int i) const { return (&x)[i]; }                               \
@@ -41,8 +65,10 @@ struct vec2 {
   vec2() : x(0), y(0) {}
   explicit vec2(real s) : x(s), y(s) {}
   vec2(real a, real b) : x(a), y(b) {}
+  explicit vec2(const ivec2& v) : x(v.x), y(v.y) {}
   GLSL_VEC_OPS(vec2, 2)
 };
+inline ivec2::ivec2(const vec2& v) : x((int)v.x), y((int)v.y) {}
 
 struct vec3 {
   real x, y, z;
@@ -93,10 +119,24 @@ GLSL_BINOPS(vec4, 4)
 struct mat4x3 {
   vec3 c[4];
   mat4x3() {}
+  explicit mat4x3(real s) {  // s on the diagonal, as GLSL's scalar matrix constructor
+    for (int i = 0; i < 3; i++) c[i][i] = s;
+  }
   mat4x3(const vec3& a, const vec3& b, const vec3& d, const vec3& e) { c[0] = a; c[1] = b; c[2] = d; c[3] = e; }
   vec3& operator[](int i) { return c[i]; }
   const vec3& operator[](int i) const { return c[i]; }
+  mat4x3& operator+=(const mat4x3& o) {
+    for (int i = 0; i < 4; i++) c[i] += o.c[i];
+    return *this;
+  }
 };
+inline mat4x3 operator+(mat4x3 a, const mat4x3& b) { return a += b; }
+// column vector times row vector: column i = col * row[i]
+inline mat4x3 outerProduct(const vec3& col, const vec4& row) {
+  mat4x3 r;
+  for (int i = 0; i < 4; i++) r.c[i] = col * row[i];
+  return r;
+}
 inline mat4x3 matrixCompMult(const mat4x3& a, const mat4x3& b) {
   mat4x3 r;
   for (int i = 0; i < 4; i++) r.c[i] = a.c[i] * b.c[i];
@@ -150,6 +190,25 @@ struct Frag {
 inline vec4 tex_off(const Tex& t, const Frag& f, const vec2& off) {
   return t.sample(vec2(f.pos.x + off.x / t.w, f.pos.y + off.y / t.h));
 }
+
+// ---------------------------------------------------------- compute passes
+// Invocation state of a compute pass.  A workgroup runs in phases: in phase
+// k every invocation executes hook() from the start until it reaches its
+// (k+1)-th barrier(), where it returns; the last phase runs every invocation
+// to the end.  So all shared-memory writes before barrier k+1 of every
+// invocation happen before any read after it -- what barrier() guarantees on
+// a GPU -- provided that re-running the earlier segments rewrites the same
+// values (true of the cooperative tile loads these shaders do before their
+// barrier).
+struct Compute {
+  uvec3 wg_id, local_id, global_id, wg_size;
+  unsigned local_index = 0;
+  Tex* out = nullptr;  // out_image
+  int bar = 0, phase = 0;
+  void store(int x, int y, const vec4& v) {
+    if (x >= 0 && y >= 0 && x < out->w && y < out->h) out->px[(size_t)y * out->w + x] = v;
+  }
+};
 
 // WIDTH/HEIGHT/WHEN reverse-Polish evaluator
 double rpn(const char* expr, const std::map<std::string, double>& env);

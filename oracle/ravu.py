@@ -27,7 +27,12 @@ import numpy as np
 
 FLT_EPS = 1.192092896e-7          # the shaders' epsilon literal
 PI = 3.141592653589793            # the shaders' pi literal
-# Relative rounding budget of an FP32 evaluation of one key (2^-24 * 256).
+# Relative rounding budget of an FP32 evaluation of one key (2^-24 * 256),
+# in units of the structure tensor's scale T = a + d (see key_margin).  The
+# CUDA kernels' key flips, measured on full-size frames, needed at most 1.5
+# units (ravu-lite-r3, 9 gradient points), 77 (ravu-r3 int11, 16 points) and
+# 137 (ravu-lite-ar-r4, 25 points summed as packed pairs with the stencil
+# scales folded into the weights); 256 covers the largest with a 1.9x factor.
 FP32_BUDGET = 256.0 * 2.0 ** -24
 REC709 = (0.2126, 0.7152, 0.0722)  # ravu-r2-rgb.hook:21 color_primary
 

@@ -1,8 +1,11 @@
 """Generate golden input/output vectors from the reference's own shader text.
 
-Builds (via ``oracle/build_ref.py``) the root ``.hook`` files listed below
-as C++ in double precision, runs them on small seeded synthetic planes and
-a few edge shapes, and stores ``tests/golden/<hook>__<case>.npz`` with
+Builds (via ``oracle/build_ref.py``) the ``.hook`` files listed below -- root
+fragment-shader files and ``compute/`` compute-shader files (ravu-3x exists
+only there) -- as C++ in double precision, runs them on small seeded
+synthetic planes and a few edge shapes, and stores
+``tests/golden/<hook>__<case>.npz`` (``compute/x`` is stored as ``compute.x``)
+with
 
 * ``input``  float32 ``[C][H][W]`` (the exact values fed to the shader),
 * ``output`` float64 ``[C][OH][OW]`` (what the shader text computed),
@@ -11,7 +14,11 @@ a few edge shapes, and stores ``tests/golden/<hook>__<case>.npz`` with
 Needs the reference checkout (default ``/root/reference``) and g++; run from
 the repository root::
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [--force]
+
+Existing files are kept unless ``--force`` is given (each case's seed is
+fixed by its position in CASES, so appended cases leave earlier ones as they
+were).
 """
 from __future__ import annotations
 
@@ -62,6 +69,20 @@ CASES = [
     ("nnedi3-nns32-win8x6", "luma", [("synth", 13, 19, 2)]),
     ("nnedi3-nns64-win8x4", "luma", [("synth", 11, 12, 2)]),
     ("nnedi3-nns128-win8x6", "luma", [("synth", 11, 12, 2)]),
+    # compute-shader forms: ravu-3x (compute only), and the compute geometry of
+    # the other families (shared-memory tiles, two-pass ravu, zoom rectangle)
+    ("compute/ravu-3x-r2", "luma", [("synth", 13, 19, 3), ("tiny", 2, 3, 3)]),
+    ("compute/ravu-3x-r3", "luma", [("synth", 13, 19, 3)]),
+    ("compute/ravu-3x-r4", "luma", [("synth", 11, 14, 3)]),
+    ("compute/ravu-3x-r2-yuv", "yuv", [("synth", 11, 14, 3)]),
+    ("compute/ravu-3x-r3-rgb", "rgb", [("synth", 11, 14, 3)]),
+    ("compute/ravu-3x-r4-yuv", "yuv", [("synth", 9, 12, 3)]),
+    ("compute/ravu-3x-r4-rgb", "rgb", [("synth", 9, 12, 3)]),
+    ("compute/ravu-lite-ar-r3", "luma", [("synth", 13, 19, 2)]),
+    ("compute/ravu-r3", "luma", [("synth", 13, 19, 2)]),
+    ("compute/ravu-r2-yuv", "yuv", [("synth", 11, 14, 2)]),
+    ("compute/ravu-zoom-ar-r2", "luma", [("x1.5", 12, 16, (24, 18))]),
+    ("compute/nnedi3-nns32-win8x6", "luma", [("synth", 13, 19, 2)]),
 ]
 
 
@@ -86,22 +107,27 @@ def run_ref(so: str, x: np.ndarray, ow: int, oh: int) -> np.ndarray:
     return out[: C * dims[0] * dims[1]].reshape(C, dims[0], dims[1])
 
 
-def main() -> int:
+def main(argv=None) -> int:
+    force = "--force" in (sys.argv[1:] if argv is None else argv)
     synth = _synth()
-    names = [c[0] for c in CASES]
-    if build_ref.main(names) != 0:
-        return 1
-    seed = 7
+    todo, seed = [], 7
     for stem, channels, cases in CASES:
-        so = os.path.join(build_ref.OUT, stem + ".so")
         for case, H, W, scale in cases:
             seed += 1
-            x = make_input(synth, channels, case, H, W, seed)
-            ow, oh = (W * scale, H * scale) if isinstance(scale, int) else scale
-            y = run_ref(so, x, ow, oh)
-            fn = os.path.join(HERE, f"{stem}__{case}.npz")
-            np.savez_compressed(fn, input=x, output=y, out_w=ow, out_h=oh)
-            print(f"{os.path.relpath(fn, REPO)}: in {x.shape} -> out {y.shape}")
+            fn = os.path.join(HERE, f"{build_ref.out_stem(stem)}__{case}.npz")
+            if force or not os.path.exists(fn):
+                todo.append((stem, channels, case, H, W, scale, seed, fn))
+    if not todo:
+        return 0
+    if build_ref.main(sorted({t[0] for t in todo})) != 0:
+        return 1
+    for stem, channels, case, H, W, scale, seed, fn in todo:
+        so = os.path.join(build_ref.OUT, build_ref.out_stem(stem) + ".so")
+        x = make_input(synth, channels, case, H, W, seed)
+        ow, oh = (W * scale, H * scale) if isinstance(scale, int) else scale
+        y = run_ref(so, x, ow, oh)
+        np.savez_compressed(fn, input=x, output=y, out_w=ow, out_h=oh)
+        print(f"{os.path.relpath(fn, REPO)}: in {x.shape} -> out {y.shape}")
     return 0
 
 

@@ -13,7 +13,8 @@ GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.n
 
 
 def _model(reference_dir, stem):
-    return models.load_model(os.path.join(reference_dir, stem + ".hook"))
+    """The model of a reference file stem; golden files name compute/x as compute.x."""
+    return models.load_model(os.path.join(reference_dir, stem.replace(".", "/") + ".hook"))
 
 
 def _run(m, x, out_w, out_h):
@@ -23,7 +24,8 @@ def _run(m, x, out_w, out_h):
 
 
 def test_golden_vectors_exist():
-    assert len(GOLDEN) >= 30
+    assert len(GOLDEN) >= 44
+    assert sum("compute.ravu-3x" in p for p in GOLDEN) >= 8   # ravu-3x exists only as compute shaders
 
 
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
