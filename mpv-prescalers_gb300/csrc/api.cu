@@ -194,7 +194,7 @@ int pz_model_create(const pz_model_desc* d, pz_model** out) {
       bias[2 * k + 1] = d->bias_b[k];
     }
     // tensor-core operand B [2*nns][KP] FP16, chunk-major: chunk c of NC
-    // neurons (NC = min(32, nns / 2)) is NC softmax-branch rows followed by
+    // neurons (NC = 32, or nns when below) is NC softmax-branch rows followed by
     // NC Elliott-branch rows.  Row = [weights (T taps), sum of the weights,
     // bias hi, bias lo, 0...]; against A rows [x_hat, mean*invstd, 1, 1, 0...]
     // the MMA yields the whole pre-activation <x,w>*invstd + b.  Softmax rows
