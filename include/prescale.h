@@ -171,8 +171,13 @@ size_t pz_scratch_bytes(const pz_model* model, const pz_plane* in, const pz_opts
 
 /* Run the full hook chain of `model` on one frame.  n_in/n_out planes are
  * 1 (luma) or 3 (yuv/rgb, planar).  Output sizes: 2x (lite, ravu, nnedi3),
- * 3x (3x), or opts->out_width x out_height (zoom).  When opts->scratch is
- * NULL and scratch is needed, it is allocated stream-ordered and freed. */
+ * 3x (3x), or opts->out_width x out_height (zoom).  ravu-lite, ravu and the
+ * column pass of nnedi3 write pixel pairs: their outputs' base and pitch must
+ * be 2-element aligned.  Scratch (pz_scratch_bytes): nnedi3 doubling both
+ * axes, the row-doubled plane (2 * W * H * element size); ravu, the FP32
+ * int11 plane between its two launches (planes * W * H * 4 bytes, 4-byte
+ * aligned).  When opts->scratch is NULL and scratch is needed, it is
+ * allocated stream-ordered and freed. */
 int pz_run(const pz_model* model, const pz_plane* in, int n_in, pz_plane* out, int n_out,
            const pz_opts* opts, void* cuda_stream);
 

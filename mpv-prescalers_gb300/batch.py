@@ -43,9 +43,10 @@ class Job:
     staging: str = "tma"   # RAVU halo staging of interior tiles: "tma" boxes or "ldg" clamped loads
 
     @staticmethod
-    def make(model: HookModel, frame, out_size=None, precision="fp32", out=None, staging="tma") -> "Job":
+    def make(model: HookModel, frame, out_size=None, precision="fp32", out=None, staging=None) -> "Job":
         """A job for ``frame`` ([H][W] or [C][H][W] CUDA tensor); allocates
-        the outputs (and NNEDI3 scratch) unless ``out`` is given."""
+        the outputs unless ``out`` is given, and the scratch the chain needs
+        (NNEDI3's row-doubled plane, the ravu lattice's int11 plane)."""
         torch = _torch()
         pl = [frame] if frame.dim() == 2 else list(frame.unbind(0))
         H, W = pl[0].shape
@@ -57,6 +58,9 @@ class Job:
         scratch = None
         if model.family == "nnedi3" and model.nnedi3_axes(W, H, (OW, OH)) == 3:
             scratch = torch.empty(2 * H * W * pl[0].element_size(), dtype=torch.uint8, device=pl[0].device)
+        elif model.family == "ravu":  # the FP32 int11 plane between the lattice launches
+            scratch = torch.empty(len(pl) * H * W * 4, dtype=torch.uint8, device=pl[0].device)
+        staging = staging or model.default_staging
         if staging not in STAGINGS:
             raise ValueError(f"staging {staging!r}: one of {sorted(STAGINGS)}")
         return Job(model, pl, outs, (OW, OH), precision, scratch, staging)

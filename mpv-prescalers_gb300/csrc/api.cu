@@ -386,12 +386,15 @@ int pz_query(const pz_model* m, int in_w, int in_h, int dtype, const pz_opts* o,
     default:
       r->out_width = 2 * in_w;
       r->out_height = 2 * in_h;
+      if (m->family == PZ_RAVU) r->scratch_bytes = pz::lattice_scratch_bytes(m, in_w, in_h);
   }
   return PZ_OK;
 }
 
 size_t pz_scratch_bytes(const pz_model* m, const pz_plane* in, const pz_opts* o) {
-  if (!m || !in || m->family != PZ_NNEDI3 || nn_axes(o) != 3) return 0;
+  if (!m || !in) return 0;
+  if (m->family == PZ_RAVU) return pz::lattice_scratch_bytes(m, in->width, in->height);
+  if (m->family != PZ_NNEDI3 || nn_axes(o) != 3) return 0;
   return (size_t)2 * in->height * in->width * dtype_size(in->dtype);
 }
 
@@ -402,7 +405,7 @@ int pz_run(const pz_model* m, const pz_plane* in, int n_in, pz_plane* out, int n
   const int C = m->channels == PZ_LUMA ? 1 : 3;
   if (n_in != C || n_out != C) return fail(PZ_EINVAL, "model needs %d planes, got %d in / %d out", C, n_in, n_out);
   int rc;
-  const bool pairs = m->family == PZ_RAVU_LITE || (m->family == PZ_NNEDI3 && (nn_axes(o) & 2));
+  const bool pairs = m->family == PZ_RAVU_LITE || m->family == PZ_RAVU || (m->family == PZ_NNEDI3 && (nn_axes(o) & 2));
   for (int c = 0; c < C; c++) {
     if ((rc = check_plane(in[c], "in", c, false)) || (rc = check_plane(out[c], "out", c, pairs))) return rc;
     if (in[c].width != in[0].width || in[c].height != in[0].height)
@@ -496,6 +499,21 @@ int pz_run(const pz_model* m, const pz_plane* in, int n_in, pz_plane* out, int n
     a.err = err;
     a.staging = o ? o->staging : 0;
     a.kp = m->kp;
+    bool own_i11 = false;
+    if (m->family == PZ_RAVU) {  // the int11 plane between the two lattice launches
+      const size_t need = pz::lattice_scratch_bytes(m, W, H);
+      if (o && o->scratch) {
+        if (o->scratch_bytes < need) return fail(PZ_EINVAL, "scratch %zu bytes < %zu needed", o->scratch_bytes, need);
+        if (reinterpret_cast<uintptr_t>(o->scratch) % 4) return fail(PZ_EINVAL, "scratch not 4-byte aligned");
+        a.i11 = static_cast<float*>(o->scratch);
+      } else {
+        void* tmp = nullptr;
+        cudaError_t e = cudaMallocAsync(&tmp, need, s);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync(scratch)");
+        a.i11 = static_cast<float*>(tmp);
+        own_i11 = true;
+      }
+    }
     switch (m->family) {
       case PZ_RAVU_LITE: rc = pz::launch_lite(a, m->radius, m->ar != 0.0f, dt, s); break;
       case PZ_RAVU_3X: rc = pz::launch_3x(a, m->radius, m->channels, dt, s); break;
@@ -503,6 +521,7 @@ int pz_run(const pz_model* m, const pz_plane* in, int n_in, pz_plane* out, int n
       case PZ_RAVU_ZOOM: rc = pz::launch_zoom(a, m->radius, m->channels, m->ar != 0.0f, dt, s); break;
       default: rc = PZ_EINVAL;
     }
+    if (own_i11) cudaFreeAsync(a.i11, s);
     if (rc) return fail(rc, "no kernel for family %d radius %d", m->family, m->radius);
   }
   cudaError_t e = cudaGetLastError();

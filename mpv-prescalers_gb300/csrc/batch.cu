@@ -121,6 +121,7 @@ int build_tables(const pz_job* jobs, int n, std::vector<pz::DevJob>* table, pz_b
     a.OW = j.out[0].width;
     a.OH = j.out[0].height;
     pz::select_lut(m, j.opts.precision, &a);
+    a.i11 = m->family == PZ_RAVU ? static_cast<float*>(j.opts.scratch) : nullptr;
     a.ar = m->ar;
     a.keys = nullptr;
     a.err = pz::device_error_word();
@@ -177,9 +178,14 @@ int validate_job(const pz_job& j, int idx) {
     case PZ_NNEDI3:
       if (m->family == PZ_NNEDI3) break;  // checked by pz_run at launch
       if (OW != 2 * W || OH != 2 * H) return pz::set_error(PZ_EINVAL, "job %d: output must be 2x the input", idx);
-      if (m->family == PZ_RAVU_LITE &&
-          ((reinterpret_cast<uintptr_t>(j.out[0].data) % (2 * es)) || (j.out[0].pitch % 2)))
-        return pz::set_error(PZ_EINVAL, "job %d: ravu-lite output must be 2-element aligned", idx);
+      for (int c = 0; c < C; c++)
+        if ((reinterpret_cast<uintptr_t>(j.out[c].data) % (2 * es)) || (j.out[c].pitch % 2))
+          return pz::set_error(PZ_EINVAL, "job %d: ravu / ravu-lite outputs must be 2-element aligned", idx);
+      if (m->family == PZ_RAVU &&
+          (!j.opts.scratch || j.opts.scratch_bytes < pz::lattice_scratch_bytes(m, W, H) ||
+           reinterpret_cast<uintptr_t>(j.opts.scratch) % 4))
+        return pz::set_error(PZ_EINVAL, "job %d: a ravu lattice job needs opts.scratch of %zu bytes (int11 plane)",
+                             idx, pz::lattice_scratch_bytes(m, W, H));
       break;
     case PZ_RAVU_3X:
       if (OW != 3 * W || OH != 3 * H) return pz::set_error(PZ_EINVAL, "job %d: output must be 3x the input", idx);

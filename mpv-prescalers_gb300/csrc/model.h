@@ -61,5 +61,13 @@ inline void select_lut(const pz_model* m, int precision, RavuArgs* a) {
   const bool h = fast_half_lut(m, precision);
   a->lut_h = h ? reinterpret_cast<const uint2*>(m->d_lut_h) : nullptr;
   a->lut_h_pitch = m->lut_h_pitch;
+  // the host's int11 texture is rgba16f: the mpv form rounds int11 to FP16,
+  // the other forms keep it FP32 between the two lattice launches
+  a->i11_half = mpv ? 1 : 0;
+}
+
+// Scratch of a ravu lattice chain: the int11 plane, FP32 [channels][H][W].
+inline size_t lattice_scratch_bytes(const pz_model* m, int W, int H) {
+  return (size_t)(m->channels == PZ_LUMA ? 1 : 3) * W * H * sizeof(float);
 }
 }  // namespace pz

@@ -201,28 +201,37 @@ __global__ void __launch_bounds__(kThreads) nn_tc_kernel(const __grid_constant__
     }
     __syncthreads();
     // ---- normalise this thread's window into its A row (pixel m = tid)
+    // The sums run as 8 independent partial sums (one per window column):
+    // the window's loads and adds form no serial chain of NT steps.
     const int m = tid, px = lane, py = warp;
     float xv[NT];
-    float sum = 0.0f;
 #pragma unroll
     for (int t = 0; t < NT; t++) {
       const int dx = t % 8 - 3, dy = t / 8 + DY0;
       const int ox = XP ? dy : dx, oy = XP ? dx : dy;
       xv[t] = tile[(py + oy - OY0) * TW + px + ox - OX0];
-      sum += xv[t];
     }
-    const float mean = sum / (float)NT;
-    float var = 0.0f;
+    float ps[8];
 #pragma unroll
-    for (int t = 0; t < NT; t++) {
-      xv[t] -= mean;
-      var += xv[t] * xv[t];
+    for (int c = 0; c < 8; c++) ps[c] = xv[c];
+#pragma unroll
+    for (int t = 8; t < NT; t++) ps[t % 8] += xv[t];
+    const float mean = (((ps[0] + ps[1]) + (ps[2] + ps[3])) + ((ps[4] + ps[5]) + (ps[6] + ps[7]))) * (1.0f / NT);
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      const float d = xv[c] - mean;
+      ps[c] = d * d;
     }
-    var /= (float)NT;
+#pragma unroll
+    for (int t = 8; t < NT; t++) {
+      const float d = xv[t] - mean;
+      ps[t % 8] = fmaf(d, d, ps[t % 8]);
+    }
+    const float var = (((ps[0] + ps[1]) + (ps[2] + ps[3])) + ((ps[4] + ps[5]) + (ps[6] + ps[7]))) * (1.0f / NT);
     const float invstd = var >= kFltEps ? rsqrtf(var) : 0.0f;
     const float stdv = var * invstd;
     const float orig = tile[(py - OY0) * TW + px - OX0];
-    {  // A row: [x_hat (NT), mean * invstd, 1, 1, 0...]
+    {  // A row: [x_hat (NT), mean * invstd, 1, 1, 0...], x_hat = x * invstd - mean * invstd
       unsigned char* row = sA + (m >> 3) * SBO + (m & 7) * 16;
       const float mterm = mean * invstd;
 #pragma unroll
@@ -231,8 +240,8 @@ __global__ void __launch_bounds__(kThreads) nn_tc_kernel(const __grid_constant__
 #pragma unroll
         for (int j = 0; j < 4; j++) {
           const int t = 8 * kc + 2 * j;
-          const float v0 = t < NT ? xv[t] * invstd : (t == NT ? mterm : (t <= NT + 2 ? 1.0f : 0.0f));
-          const float v1 = t + 1 < NT ? xv[t + 1] * invstd
+          const float v0 = t < NT ? fmaf(xv[t], invstd, -mterm) : (t == NT ? mterm : (t <= NT + 2 ? 1.0f : 0.0f));
+          const float v1 = t + 1 < NT ? fmaf(xv[t + 1], invstd, -mterm)
                                       : (t + 1 == NT ? mterm : (t + 1 <= NT + 2 ? 1.0f : 0.0f));
           h[j] = __floats2half2_rn(v0, v1);
         }

@@ -1,7 +1,7 @@
 // Per-model launches of the ravu lattice chain (ravu_tiles.cuh): the int11
-// tile program, then the int10/int01 program, which reads int11 back from
-// the output plane -- the four passes of ravu-r3.hook:15-437 in two launches
-// with no intermediate plane outside the output.
+// tile program writes the compact FP32 int11 plane (caller scratch), the
+// int10/int01 program reads it and writes every output pixel -- the four
+// passes of ravu-r3.hook:15-437 in two launches.
 #include "ravu_tiles.cuh"
 
 namespace pz {

@@ -189,7 +189,9 @@ struct LiteTile {
   static constexpr int N = 2 * R - 1, S = N * N, HALO = R - 1;
   static constexpr int TW = kTileW + N - 1, TH = kTileH + N - 1;
   // the value tile; the anti-ringing powers are formed per tap in registers
-  // (ar_pow2)
+  // (ar_pow2): a shared table of each texel's four powers, formed once per
+  // texel, measured 2-13 % slower (an extra barrier, 8 KB more shared memory
+  // per CTA and a 16-byte shared load per tap)
   static constexpr size_t smem_bytes = (size_t)((TW * TH + 3) & ~3) * 4;
 
   static constexpr int kPlanes = 1;
@@ -423,11 +425,10 @@ __device__ __forceinline__ void ravu_filter(const float4* L, const Val& val, flo
 }
 
 // ------------------------------------------------------ ravu lattice -----
-// int11: the keyed filter over the input window.  Writes int11 and the input
-// copy straight into the output plane at (2i+1, 2j+1) and (2i, 2j).
-// ------------------------------------------------------ ravu lattice -----
-// int11: the keyed filter over the input window.  Writes int11 and the input
-// copy straight into the output plane at (2i+1, 2j+1) and (2i, 2j).
+// int11: the keyed filter over the input window (ravu-r3.hook:15-146).  Each
+// thread stores its pixel's int11 value into the compact FP32 int11 plane
+// (p.i11, [C][H][W]): one coalesced 4-byte store per channel.  The lattice
+// program below writes every output pixel.
 template <int R, int CM, typename T>
 struct Int11Tile {
   static constexpr int N = 2 * R, S = N * N, HALO = R - 1;
@@ -460,12 +461,12 @@ struct Int11Tile {
     const float4* L = p.lut + (size_t)min(max(key, 0), p.lut_rows - 1) * p.lut_cols;
     float res[C];
     ravu_filter<S, C>(L, val, res);
+    const size_t plane = (size_t)p.W * p.H;
 #pragma unroll
     for (int c = 0; c < C; c++) {
-      T* o = static_cast<T*>(p.out[c]);
-      const size_t op = p.out_pitch[c];
-      stp(o + (size_t)(2 * gy) * op + 2 * gx, tile[c * TW * TH + (ty + HALO) * TW + tx + HALO]);
-      stp(o + (size_t)(2 * gy + 1) * op + 2 * gx + 1, clampf(res[c], 0.f, 1.f));
+      float v = clampf(res[c], 0.f, 1.f);
+      if (p.i11_half) v = __half2float(__float2half_rn(v));
+      p.i11[c * plane + (size_t)gy * p.W + gx] = v;
     }
   }
 };
@@ -491,9 +492,11 @@ __host__ __device__ constexpr int lat_dy(int k, int L) {
                 : (lat_src<N>(k, L) == 0 ? (k % N - k / N + 1) / 2 : (k % N - k / N) / 2);
 }
 
-// int10 + int01: both lattice filters per input pixel.  The int11 tile is
-// read back from the output plane at clamped int11 coordinates (the
-// clamp-to-edge of the int11 texture).
+// int10 + int01: both lattice filters per input pixel (ravu-r3.hook:148-437).
+// The input tile and the int11 tile (from the FP32 int11 plane, clamped to
+// its edge: the clamp-to-edge of the int11 texture) are staged; each thread
+// then holds all four samples of its output 2x2 block -- input (0,0), int10
+// (1,0), int01 (0,1), int11 (1,1) -- and writes them as two pixel-pair rows.
 template <int R, int CM, typename T>
 struct LatticeTile {
   static constexpr int N = 2 * R, S = N * N;
@@ -513,13 +516,14 @@ struct LatticeTile {
     float* t11 = smem + PL * TW * TH;       // int11, offsets -R .. R-1
     float* l11 = t11 + C * TW * TH;
     if (!stage_frame<CM, TW, TH, T>(p, tma, x0 - (R - 1), y0 - (R - 1), tin, lin)) return;
+    const size_t plane = (size_t)p.W * p.H;
     for (int i = threadIdx.x; i < TW * TH; i += kTileThreads) {
       const int ty = i / TW, tx = i % TW;
       const int cx = clampi(x0 - R + tx, 0, p.W - 1), cy = clampi(y0 - R + ty, 0, p.H - 1);
       float v[3] = {0.f, 0.f, 0.f};
 #pragma unroll
       for (int c = 0; c < C; c++) {
-        v[c] = ldp(static_cast<const T*>(p.out[c]) + (size_t)(2 * cy + 1) * p.out_pitch[c] + 2 * cx + 1);
+        v[c] = __ldg(p.i11 + c * plane + (size_t)cy * p.W + cx);
         t11[c * TW * TH + i] = v[c];
       }
       if (CM == kRgb) l11[i] = rgb_luma(v[0], v[1], v[2]);
@@ -528,6 +532,7 @@ struct LatticeTile {
     const int tx = threadIdx.x % kTileW, ty = threadIdx.x / kTileW;
     const int gx = x0 + tx, gy = y0 + ty;
     if (gx >= p.W || gy >= p.H) return;
+    float res[2][C];
 #pragma unroll
     for (int L = 0; L < 2; L++) {
       auto idx = [&](int k) {
@@ -545,17 +550,14 @@ struct LatticeTile {
       const int key = ravu_key(a, b, d, p.kp);
       if (p.keys) p.keys[(size_t)(1 + L) * p.W * p.H + (size_t)gy * p.W + gx] = key;
       const float4* Lr = p.lut + (size_t)min(max(key, 0), p.lut_rows - 1) * p.lut_cols;
-      float res[C];
-      ravu_filter<S, C>(Lr, val, res);
+      ravu_filter<S, C>(Lr, val, res[L]);
+    }
 #pragma unroll
-      for (int c = 0; c < C; c++) {
-        T* o = static_cast<T*>(p.out[c]);
-        const size_t op = p.out_pitch[c];
-        if (L == 0)
-          stp(o + (size_t)(2 * gy) * op + 2 * gx + 1, clampf(res[c], 0.f, 1.f));  // int10
-        else
-          stp(o + (size_t)(2 * gy + 1) * op + 2 * gx, clampf(res[c], 0.f, 1.f));  // int01
-      }
+    for (int c = 0; c < C; c++) {
+      T* o = static_cast<T*>(p.out[c]) + (size_t)(2 * gy) * p.out_pitch[c] + 2 * gx;
+      // row 2i: input, int10; row 2i+1: int01, int11 (ravu-r3.hook:424-437)
+      stp2(o, tin[c * TW * TH + (ty + R - 1) * TW + tx + R - 1], clampf(res[0][c], 0.f, 1.f));
+      stp2(o + p.out_pitch[c], clampf(res[1][c], 0.f, 1.f), t11[c * TW * TH + (ty + R) * TW + tx + R]);
     }
   }
 };
@@ -610,7 +612,11 @@ __device__ __forceinline__ float comp4(const float4& v, int i) {
 }
 
 // One thread per OUTPUT pixel; the tile is 32 x 8 output pixels and stages the
-// input rectangle they touch (at most (32+N+1) x (8+N+1) when upscaling).
+// input rectangle they touch (at most (32+N+1) x (8+N+1) when upscaling;
+// its origin follows from the tile's source positions, as the compute
+// shader's rect, compute/ravu-zoom-ar-r2.hook:28-37), by clamped loads of
+// just that rectangle: a fixed-size TMA box of the largest rectangle
+// converts up to 1.6x more texels at 1.5x and measured slower.
 template <int R, int CM, bool AR, typename T, bool H16 = false>
 struct ZoomTile {
   static constexpr int N = 2 * R, S = N * N, LO = R - 1;
@@ -622,7 +628,7 @@ struct ZoomTile {
   static constexpr size_t smem_bytes =
       (size_t)(C + (CM == kRgb ? 1 : 0)) * RW * RH * 4 + (kTileW + kTileH) * sizeof(ZoomPos);
 
-  static constexpr int kPlanes = 0;  // the input rectangle moves with the ratio: clamped loads only
+  static constexpr int kPlanes = 0;  // clamped loads only
   static constexpr int kMinBlocks = 0;  // no launch-bounds minimum
   using Elem = T;
 

@@ -5,7 +5,7 @@ frames a player's render loop would hand to the hook chain).  The server
 
 * keeps every model's LUT / weights resident on the device;
 * admits queued requests in arrival order while the device-memory they need
-  (input + output planes + NNEDI3 scratch) fits the HBM budget and an
+  (input + output planes + scratch) fits the HBM budget and an
   execution slot is free -- requests arriving while others run are admitted
   as soon as memory and slots free up;
 * runs each admitted request on its slot's CUDA stream (host->device copy,
@@ -71,6 +71,8 @@ def request_bytes(model: HookModel, frame, out_size) -> int:
     nbytes = C * (H * W + OH * OW) * es
     if model.family == "nnedi3" and model.nnedi3_axes(W, H, (OW, OH)) == 3:
         nbytes += 2 * H * W * es
+    elif model.family == "ravu":   # the FP32 int11 plane between the lattice launches
+        nbytes += C * H * W * 4
     return nbytes
 
 
@@ -263,13 +265,15 @@ def warmup_trace(models: Dict[str, HookModel], resolutions=RESOLUTIONS, algorith
 
 def poisson_trace(models: Dict[str, HookModel], n: int, rate: float = 240.0, streams: int = 64,
                   seed: int = 5000, precision: str = "fast", frame_pool: int = 2,
-                  resolutions=RESOLUTIONS, algorithms=ALGORITHMS, out_ring: int = 0) -> List[Request]:
+                  resolutions=RESOLUTIONS, algorithms=ALGORITHMS, out_ring: int = 3) -> List[Request]:
     """Poisson arrivals at `rate` frames/s over `streams` streams; resolution
     and algorithm drawn per stream (the mix of the serving configuration).
     Frames come from a small pool of seeded synthetic frames per resolution.
-    ``out_ring`` > 0 gives every stream that many pinned output frames,
-    reused in turn (a player's own frame buffers); 0 lets the server
-    allocate one per request."""
+    ``out_ring`` > 0 (default 3) gives every stream that many pinned output
+    frames, reused in turn -- a player's own frame buffers, made before the
+    trace runs; 0 lets the server page-lock a new host frame per request,
+    which puts tens of MB of page-locking on the request path of every
+    2160p result and dominates the latency tail."""
     from . import synth
     torch = _torch()
     rng = np.random.default_rng(seed)

@@ -55,9 +55,22 @@ def _psnr(a, b):
     return float("inf") if mse == 0 else 10.0 * np.log10(1.0 / mse)
 
 
-def _run_gpu(hm, x, out_size, dtype=torch.float32, precision="fp32"):
+def _run_gpu(hm, x, out_size, dtype=torch.float32, precision="fp32", int11=None):
+    """The GPU's output and raw keys; for the ravu lattice with `int11` a
+    list, also the FP32 int11 plane it kept between its two launches (the
+    caller scratch passed in opts.scratch)."""
     xt = torch.from_numpy(np.ascontiguousarray(x)).to("cuda", dtype)
-    y, keys = hm.upscale(xt, out_size=out_size, precision=precision, return_keys=True)
+    if hm.family != "ravu" or int11 is None:
+        y, keys = hm.upscale(xt, out_size=out_size, precision=precision, return_keys=True)
+    else:
+        C, H, W = xt.shape
+        scratch = torch.empty((C, H, W), dtype=torch.float32, device="cuda")
+        y = torch.empty((C, 2 * H, 2 * W), dtype=dtype, device="cuda")
+        keys = torch.empty(hm.key_shape(W, H, 2 * W, 2 * H), dtype=torch.int32, device="cuda")
+        hm.run_raw(list(xt.unbind(0)), list(y.unbind(0)), out_size=(2 * W, 2 * H), precision=precision,
+                   keys=keys, scratch=scratch)
+        torch.cuda.synchronize()
+        int11.append(scratch.double().cpu().numpy())
     torch.cuda.synchronize()
     return y.float().cpu().numpy().astype(np.float64), keys.cpu().numpy()
 
@@ -98,14 +111,17 @@ def _check_keyed(hm, x, out_size, tol=TOL_FP32, dtype=torch.float32, precision="
     """Keys and values of the GPU against the oracle.
 
     For the ravu lattice the int10/int01 passes read int11; they are checked
-    on the GPU's own int11 plane so that each pass is compared on identical
-    inputs (the int11 pass itself is checked on the original input).
+    on the GPU's own int11 plane (the FP32 plane it keeps between its two
+    launches, taken from the scratch the test passes in), so that each pass
+    is compared on identical inputs (the int11 pass itself is checked on the
+    original input).
     Returns the key figures (``key_stats``) plus the max-abs with identical
     keys and the max-abs and PSNR against the unforced oracle.
     """
     m = hm.model if oracle_model is None else oracle_model
-    y, kg = _run_gpu(hm, x, out_size, dtype=dtype, precision=precision)
-    over = y[:, 1::2, 1::2] if m.family == "ravu" else None
+    planes11 = []
+    y, kg = _run_gpu(hm, x, out_size, dtype=dtype, precision=precision, int11=planes11)
+    over = planes11[0] if planes11 else None
     ref, info = oracle.keyed_upscale(m, x, out_size, int11=over)
     forced, _ = oracle.keyed_upscale(m, x, out_size, keys=kg, int11=over)
     assert y.shape == ref.shape

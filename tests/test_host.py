@@ -65,7 +65,7 @@ def test_plan_cache_key_is_order_free_and_shape_sensitive():
 
 @pytest.mark.parametrize("name,shape,osz,want,scratch", [
     ("ravu-lite-ar-r3", (36, 52), None, (72, 104), None),
-    ("ravu-r4-rgb", (20, 30), None, (40, 60), None),
+    ("ravu-r4-rgb", (20, 30), None, (40, 60), 3 * 20 * 30 * 4),       # the FP32 int11 plane
     ("ravu-3x-r3-yuv", (20, 30), None, (60, 90), None),
     ("ravu-zoom-ar-r2", (30, 40), (70, 51), (51, 70), None),
     ("nnedi3-nns16-win8x4", (20, 30), None, (40, 60), 2 * 20 * 30 * 2),
@@ -105,7 +105,8 @@ def test_request_bytes():
     assert S.request_bytes(lite, f, None) == (100 * 200 + 200 * 400) * 2
     rgb, _ = synth.model_for("ravu-r4-rgb")
     f3 = torch.zeros((3, 100, 200), dtype=torch.float32)
-    assert S.request_bytes(rgb, f3, None) == 3 * (100 * 200 + 200 * 400) * 4
+    # planes in and out, plus the FP32 int11 plane of the lattice
+    assert S.request_bytes(rgb, f3, None) == 3 * (100 * 200 + 200 * 400) * 4 + 3 * 100 * 200 * 4
     nn, _ = synth.model_for("nnedi3-nns64-win8x4")
     assert S.request_bytes(nn, f, None) == (100 * 200 + 200 * 400 + 2 * 100 * 200) * 2
     zoom, _ = synth.model_for("ravu-zoom-ar-r2")
@@ -268,4 +269,7 @@ def test_trace_output_rings_are_per_stream_and_shaped():
         assert len({o.data_ptr() for o in outs}) == min(3, len(outs))
         for i in range(3, len(outs)):
             assert outs[i] is outs[i - 3]
-    assert all(r.output is None for r in S.poisson_trace(models, 20, resolutions=res, seed=3))
+    # the default is a ring of 3 caller frames per stream; 0 leaves the
+    # result frames to the server
+    assert all(r.output is not None for r in S.poisson_trace(models, 20, resolutions=res, seed=3))
+    assert all(r.output is None for r in S.poisson_trace(models, 20, resolutions=res, seed=3, out_ring=0))
