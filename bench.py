@@ -567,6 +567,29 @@ def run_gpu(args, refs=None):
             "jobs": len(jobs), "ms": ms, "out_mpix_s": out_px / (ms / 1e3) / 1e6, "strategy": ex.strategy,
             "form": "FP16 planes, fast form"}
         del ex, jobs
+        # one tick of a 64-stream player: a frame of each stream through the
+        # serving mix (resolutions 480p-2160p, ravu-lite-ar-r3 / ravu-r4-yuv /
+        # nnedi3-nns64-win8x4 / ravu-zoom-ar-r2 at 1.75x), FP16, fast form:
+        # one launch chain per frame against the persistent batch replayed
+        # from a CUDA graph, and the strategy the autotuner picks
+        from mpv_prescalers_gb300 import serve
+        tick_models = {name: synth.model_for(name)[0] for name, _ in serve.ALGORITHMS}
+        tick = serve.poisson_trace(tick_models, 64, rate=1e6, streams=64, frame_pool=1, seed=5002, out_ring=0)
+        tjobs = [_batch.Job.make(tick_models[r.model], r.frame.to(dev), out_size=r.out_size, precision="fast")
+                 for r in tick]
+        per_job_ms = _batch._time_ms(lambda: _batch.run_per_job(tjobs), 5)
+        tb = _batch.Batch(tjobs)
+        tb.launch()
+        tb.capture()
+        batch_ms = _batch._time_ms(tb.replay, 5)
+        tb.close()
+        strategy, ttimes = _batch.autotune(tjobs, cache=_batch.PlanCache(os.path.join(tempfile.mkdtemp(), "p.json")))
+        tick_px = sum(j.outputs[0].shape[-1] * j.outputs[0].shape[-2] * len(j.outputs) for j in tjobs)
+        configs["serving_tick_64_frames"] = {
+            "frames": len(tjobs), "per_job_ms": per_job_ms, "batch_graph_ms": batch_ms,
+            "batch_vs_per_job": per_job_ms / batch_ms, "autotuned": strategy, "times_ms": ttimes,
+            "out_mpix_s_batch": tick_px / (batch_ms / 1e3) / 1e6}
+        del tjobs
         # NNEDI3 nns128-win8x6 on 4 frames of 1280x720, fast vs plain FP32
         nm = models["nnedi3-nns128-win8x6"]
         res = {}
@@ -597,7 +620,12 @@ def run_gpu(args, refs=None):
         serve.Server(smodels).run(serve.warmup_trace(smodels))
         # each stream's output frames are the caller's (a ring of 3 pinned
         # buffers per stream, the default); the same trace with one host
-        # frame page-locked per request is reported beside it
+        # frame page-locked per request is reported beside it.  Each measured
+        # trace follows an untimed run of a trace of the same shape, so the
+        # device allocator already holds what concurrent requests need (a
+        # steady-state server; growing it mid-trace synchronises the device)
+        warm = dict(n=args.serve_requests, streams=64, frame_pool=1)
+        serve.Server(smodels, hbm_budget=40e9, slots=8).run(serve.poisson_trace(smodels, rate=4800.0, **warm))
         trace = serve.poisson_trace(smodels, args.serve_requests, rate=240.0, streams=64, frame_pool=1)
         served = serve.Server(smodels, hbm_budget=40e9, slots=8).run(trace)
         alloc_trace = serve.poisson_trace(smodels, args.serve_requests, rate=240.0, streams=64, frame_pool=1,

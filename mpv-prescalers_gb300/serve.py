@@ -215,7 +215,13 @@ def serial_baseline(models: Dict[str, HookModel], trace: Sequence[Request]) -> D
     clock = 0.0
     done = []
     host_out: Dict[Tuple, "torch.Tensor"] = {}   # one pinned result buffer per shape, made before timing
-    reqs = [Request(r.rid, r.stream_id, r.model, _pinned(r.frame.float()), r.arrival, r.out_size, "fp32")
+    fp32: Dict[int, "torch.Tensor"] = {}          # one pinned FP32 copy per distinct trace frame
+
+    def as_fp32(f):
+        if id(f) not in fp32:
+            fp32[id(f)] = _pinned(f.float())
+        return fp32[id(f)]
+    reqs = [Request(r.rid, r.stream_id, r.model, as_fp32(r.frame), r.arrival, r.out_size, "fp32")
             for r in sorted(trace, key=lambda q: q.arrival)]
     for q in reqs:
         m = models[q.model]
