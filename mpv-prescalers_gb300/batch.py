@@ -31,6 +31,16 @@ def _torch():
     return torch
 
 
+def scratch_bytes(model: HookModel, W: int, H: int, planes: int, elem: int, out_size) -> int:
+    """Device scratch of one frame's chain: NNEDI3 doubling both axes, the
+    row-doubled plane; ravu (lattice), the FP32 int11 plane; else 0."""
+    if model.family == "nnedi3" and model.nnedi3_axes(W, H, out_size) == 3:
+        return 2 * H * W * elem
+    if model.family == "ravu":
+        return planes * H * W * 4
+    return 0
+
+
 @dataclass
 class Job:
     """One frame through one model: planes are lists of [H][W] CUDA tensors."""
@@ -43,10 +53,12 @@ class Job:
     staging: str = "tma"   # RAVU halo staging of interior tiles: "tma" boxes or "ldg" clamped loads
 
     @staticmethod
-    def make(model: HookModel, frame, out_size=None, precision="fp32", out=None, staging=None) -> "Job":
+    def make(model: HookModel, frame, out_size=None, precision="fp32", out=None, staging=None,
+             scratch=None) -> "Job":
         """A job for ``frame`` ([H][W] or [C][H][W] CUDA tensor); allocates
         the outputs unless ``out`` is given, and the scratch the chain needs
-        (NNEDI3's row-doubled plane, the ravu lattice's int11 plane)."""
+        (NNEDI3's row-doubled plane, the ravu lattice's int11 plane) unless
+        ``scratch`` (a uint8 tensor of at least ``scratch_bytes``) is given."""
         torch = _torch()
         pl = [frame] if frame.dim() == 2 else list(frame.unbind(0))
         H, W = pl[0].shape
@@ -55,11 +67,11 @@ class Job:
             outs = list(torch.empty((len(pl), OH, OW), dtype=pl[0].dtype, device=pl[0].device).unbind(0))
         else:
             outs = [out] if out.dim() == 2 else list(out.unbind(0))
-        scratch = None
-        if model.family == "nnedi3" and model.nnedi3_axes(W, H, (OW, OH)) == 3:
-            scratch = torch.empty(2 * H * W * pl[0].element_size(), dtype=torch.uint8, device=pl[0].device)
-        elif model.family == "ravu":  # the FP32 int11 plane between the lattice launches
-            scratch = torch.empty(len(pl) * H * W * 4, dtype=torch.uint8, device=pl[0].device)
+        need = scratch_bytes(model, W, H, len(pl), pl[0].element_size(), (OW, OH))
+        if scratch is None and need:
+            scratch = torch.empty(need, dtype=torch.uint8, device=pl[0].device)
+        elif scratch is not None and scratch.numel() < need:
+            raise ValueError(f"scratch of {scratch.numel()} bytes, the chain needs {need}")
         staging = staging or model.default_staging
         if staging not in STAGINGS:
             raise ValueError(f"staging {staging!r}: one of {sorted(STAGINGS)}")

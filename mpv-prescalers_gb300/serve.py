@@ -102,7 +102,21 @@ class _Slot:
     reqs: List[Request] = field(default_factory=list)
     done: Optional["torch.cuda.Event"] = None
     nbytes: int = 0
-    keep: list = field(default_factory=list)   # device tensors of the in-flight requests
+    keep: list = field(default_factory=list)   # objects of the in-flight requests
+    # the slot's device arena: every in-flight request's input, output and
+    # scratch planes are carved from it; it grows only when an admitted group
+    # needs more, so a server in steady state allocates nothing per request
+    # (a device allocation mid-trace synchronises the whole device)
+    arena: Optional["torch.Tensor"] = None
+
+
+def _carve(arena, off: int, shape, dtype):
+    """A tensor of `shape` / `dtype` at byte offset `off` of `arena`
+    (256-byte aligned); returns it and the next offset."""
+    torch = _torch()
+    n = int(np.prod(shape)) * torch.empty((), dtype=dtype).element_size()
+    t = arena[off:off + n].view(dtype).view(tuple(shape))
+    return t, off + ((n + 255) & ~255)
 
 
 class Server:
@@ -122,17 +136,44 @@ class Server:
         self.peak = 0
         self.rejected: List[Request] = []
 
+    def _arena_bytes(self, reqs: List[Request]) -> int:
+        n = 0
+        for r in reqs:
+            m = self.models[r.model]
+            C, H, W = r.frame.shape
+            OW, OH = m.output_size(W, H, r.out_size)
+            es = r.frame.element_size()
+            for b in (C * H * W * es, C * OH * OW * es,
+                      _batch.scratch_bytes(m, W, H, C, es, (OW, OH))):
+                n += (b + 255) & ~255
+        return n
+
     # -- one admitted group on one slot ------------------------------------
     def _launch(self, slot: _Slot, reqs: List[Request], now: float):
         torch = _torch()
         jobs = []
+        need = self._arena_bytes(reqs)
+        if slot.arena is None or slot.arena.numel() < need:
+            # the slot is idle here (retired before admission), so the old
+            # arena can go; the new one is allocated once for all later groups
+            slot.arena = None
+            slot.arena = torch.empty(need, dtype=torch.uint8, device=self.device)
+        off = 0
         with torch.cuda.stream(slot.stream):
             for r in reqs:
                 m = self.models[r.model]
-                xd = r.frame.to(self.device, non_blocking=True)
-                job = _batch.Job.make(m, xd, out_size=r.out_size, precision=r.precision)
+                C, H, W = r.frame.shape
+                OW, OH = m.output_size(W, H, r.out_size)
+                xd, off = _carve(slot.arena, off, (C, H, W), r.frame.dtype)
+                xd.copy_(r.frame, non_blocking=True)
+                out, off = _carve(slot.arena, off, (C, OH, OW), r.frame.dtype)
+                sb = _batch.scratch_bytes(m, W, H, C, r.frame.element_size(), (OW, OH))
+                scratch = None
+                if sb:
+                    scratch, off = _carve(slot.arena, off, (sb,), torch.uint8)
+                job = _batch.Job.make(m, xd, out_size=r.out_size, precision=r.precision,
+                                      out=out if C > 1 else out[0], scratch=scratch)
                 jobs.append(job)
-                slot.keep += [xd] + job.outputs + ([job.scratch] if job.scratch is not None else [])
             if self.mode == "batch" and len(jobs) > 1:
                 b = _batch.Batch(jobs, stream=slot.stream)
                 b.launch(stream=slot.stream)
