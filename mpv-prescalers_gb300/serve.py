@@ -148,6 +148,20 @@ class Server:
                 n += (b + 255) & ~255
         return n
 
+    def reserve(self, trace: Sequence[Request], max_group: int = 4) -> int:
+        """Size every slot's device arena for the largest group of `trace`'s
+        requests it could be handed (a server set up for the frame sizes it
+        serves), so that serving allocates nothing; returns the bytes per slot."""
+        torch = _torch()
+        per = sorted((self._arena_bytes([r]) for r in trace), reverse=True)
+        need = sum(per[:max_group if self.mode == "batch" else 1])
+        for s in self.slots:
+            if s.arena is None or s.arena.numel() < need:
+                s.arena = None
+                s.arena = torch.empty(need, dtype=torch.uint8, device=self.device)
+        torch.cuda.synchronize(self.device)
+        return need
+
     # -- one admitted group on one slot ------------------------------------
     def _launch(self, slot: _Slot, reqs: List[Request], now: float):
         torch = _torch()

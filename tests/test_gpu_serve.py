@@ -25,6 +25,9 @@ def test_each_result_same_alone_and_in_the_mix(models, mode, ring):
                                 out_ring=ring)
     given = [r.output for r in trace]
     srv = serve.Server(models, hbm_budget=40e9, slots=6, mode=mode)
+    if ring:   # arenas sized up front: the run then allocates nothing on the device
+        per_slot = srv.reserve(trace)
+        assert all(s.arena.numel() == per_slot for s in srv.slots)
     stats = srv.run(trace)
     assert stats["requests"] == len(trace)
     for r in trace:
