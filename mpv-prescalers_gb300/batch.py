@@ -170,9 +170,43 @@ def run_per_job(jobs: Sequence[Job], stream=None):
                         scratch=j.scratch)
 
 
+_STREAM_POOL: Dict[Tuple[int, int], "torch.cuda.Stream"] = {}
+
+
+def _pool_stream(device, k: int):
+    """Side stream k of `device`, created once and kept for the process."""
+    torch = _torch()
+    key = (device.index if device.index is not None else torch.cuda.current_device(), k)
+    if key not in _STREAM_POOL:
+        _STREAM_POOL[key] = torch.cuda.Stream(device)
+    return _STREAM_POOL[key]
+
+
+def run_streams(jobs: Sequence[Job], stream=None, max_streams: int = 4):
+    """The co-scheduled strategy: the jobs of each model go on their own side
+    stream (forked from and joined back to `stream`), one pz_run chain per
+    job, so that the programs of different models run at the same time and
+    fill each other's idle issue slots (e.g. an issue-bound program beside a
+    shared-memory-bound one).  Capturable in a CUDA graph (fork and join are
+    stream waits)."""
+    torch = _torch()
+    dev = jobs[0].inputs[0].device
+    main = stream if stream is not None else torch.cuda.current_stream(dev)
+    groups: Dict[str, List[Job]] = {}
+    for j in jobs:
+        groups.setdefault(j.model.name, []).append(j)
+    side = [_pool_stream(dev, k) for k in range(min(max_streams, len(groups)))]
+    for s in side:
+        s.wait_stream(main)
+    for i, (_, g) in enumerate(sorted(groups.items())):
+        run_per_job(g, stream=side[i % len(side)])
+    for s in side:
+        main.wait_stream(s)
+
+
 # ------------------------------------------------------------ autotuner ----
 
-STRATEGIES = ("per_job", "batch:1", "batch:2", "batch:0")
+STRATEGIES = ("per_job", "streams", "batch:1", "batch:2", "batch:0")
 
 
 def _default_cache_path() -> str:
@@ -266,6 +300,8 @@ def autotune(jobs: Sequence[Job], cache: Optional[PlanCache] = None, reps: int =
     for st in strategies:
         if st == "per_job":
             times[st] = _time_ms(lambda: run_per_job(jobs), reps)
+        elif st == "streams":
+            times[st] = _time_ms(lambda: run_streams(jobs), reps)
         else:
             b = Batch(jobs, ctas_per_sm=int(st.split(":")[1]))
             times[st] = _time_ms(b.launch, reps)
@@ -280,18 +316,37 @@ class Executor:
 
     def __init__(self, jobs: Sequence[Job], cache: Optional[PlanCache] = None, tune: bool = True,
                  use_graph: bool = True):
+        torch = _torch()
         self.jobs = list(jobs)
         self.strategy = autotune(self.jobs, cache)[0] if tune else "batch:0"
         self.batch = None
         self.graph = None
-        if self.strategy != "per_job":
+        if self.strategy.startswith("batch:"):
             self.batch = Batch(self.jobs, ctas_per_sm=int(self.strategy.split(":")[1]))
             if use_graph:
                 self.batch.launch()
                 self.batch.capture()
+        elif self.strategy == "streams" and use_graph:
+            # the fork / join of the side streams is recorded into the graph
+            dev = self.jobs[0].inputs[0].device
+            run_streams(self.jobs)   # every kernel loaded before capture
+            cur = torch.cuda.current_stream(dev)
+            s = torch.cuda.Stream(dev)
+            s.wait_stream(cur)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.stream(s):
+                g.capture_begin()
+                run_streams(self.jobs, stream=s)
+                g.capture_end()
+            cur.wait_stream(s)
+            self.graph = g
 
     def run(self):
-        if self.batch is None:
+        if self.graph is not None:
+            self.graph.replay()
+        elif self.strategy == "streams":
+            run_streams(self.jobs)
+        elif self.batch is None:
             run_per_job(self.jobs)
         elif self.batch.graph is not None:
             self.batch.replay()

@@ -99,6 +99,29 @@ def test_autotuner_picks_and_caches(tmp_path):
             assert torch.equal(o, e)
 
 
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_co_scheduled_streams_match_per_frame_launches(use_graph, tmp_path):
+    """The co-scheduled strategy (each model's jobs on their own side stream,
+    forked from and joined to the caller's stream; replayed from a CUDA graph
+    or launched directly) gives the per-frame pixels bit for bit."""
+    jobs = _jobs()
+    want = _expected(jobs)
+    for j in jobs:
+        for o in j.outputs:
+            o.zero_()
+    cache = B.PlanCache(str(tmp_path / "plans.json"))
+    key = B.PlanCache.key(torch.cuda.get_device_name(0), jobs)
+    cache.put(key, {"strategy": "streams", "times_ms": {}})
+    ex = B.Executor(jobs, cache=cache, use_graph=use_graph)
+    assert ex.strategy == "streams" and (ex.graph is not None) == use_graph
+    for _ in range(2):
+        ex.run()
+    torch.cuda.synchronize()
+    for j, w in zip(jobs, want):
+        for o, e in zip(j.outputs, w):
+            assert torch.equal(o, e), j.model.name
+
+
 def test_ragged_random_batches_match_per_frame_launches():
     """Many small and odd-sized frames of every family in every form: the
     per-program persistent groups give the per-frame pixels bit for bit."""
