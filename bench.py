@@ -67,6 +67,17 @@ def _pkg():
     return _entry._package()
 
 
+def _layouts(jobs):
+    """The tile layout ("staging/rows") each distinct model and frame shape of
+    a job list runs."""
+    out = {}
+    for j in jobs:
+        p = j.inputs[0]
+        k = f"{j.model.name} {p.shape[1]}x{p.shape[0]}->{j.out_size[0]}x{j.out_size[1]}"
+        out[k] = f"{j.staging}/{j.tile_rows or 'default'}"
+    return out
+
+
 # ------------------------------------------------------------------ CPU ---
 
 _FRAME = {}   # per worker process: the synthetic frame of each seed, made before timing
@@ -556,6 +567,16 @@ def run_gpu(args, refs=None):
                        "batched_mpix_s": res["batched"], "batched_ratio": res["batched"] / res["fp32"],
                        "batched": f"{NFRAMES} FP16 frames per persistent launch, CUDA graph replay"}
 
+    # ---- tile layouts of the workload's programs: every tile height x halo
+    # staging of one 1080p FP16 frame, fast form (batch.autotune_tiles)
+    import tempfile
+    from mpv_prescalers_gb300 import batch as _batch
+    tile_sweep = {}
+    tcache = _batch.PlanCache(os.path.join(tempfile.mkdtemp(), "tiles.json"))
+    for n in MODELS:
+        (st, rows), t = _batch.autotune_tiles(models[n], x16[0], precision="fast", cache=tcache, reps=10)
+        tile_sweep[n] = {"best": f"{st}/{rows}", "us": {k: round(v * 1e3, 1) for k, v in t.items()}}
+
     # ---- precision of each configuration against the FP64 oracle
     precision = precision_figures(models, refs, dev) if refs else None
 
@@ -593,7 +614,7 @@ def run_gpu(args, refs=None):
         ms = a.elapsed_time(b) / 3
         configs["zoom_rgb_1.5x_2.25x_plus_ravu_r4_yuv_16_frames_each"] = {
             "jobs": len(jobs), "ms": ms, "out_mpix_s": out_px / (ms / 1e3) / 1e6, "strategy": ex.strategy,
-            "form": "FP16 planes, fast form"}
+            "tile_layouts": _layouts(ex.jobs), "form": "FP16 planes, fast form"}
         del ex, jobs
         # one tick of a 64-stream player: a frame of each stream through the
         # serving mix (resolutions 480p-2160p, ravu-lite-ar-r3 / ravu-r4-yuv /
@@ -611,12 +632,18 @@ def run_gpu(args, refs=None):
         tb.capture()
         batch_ms = _batch._time_ms(tb.replay, 5)
         tb.close()
-        strategy, ttimes = _batch.autotune(tjobs, cache=_batch.PlanCache(os.path.join(tempfile.mkdtemp(), "p.json")))
+        tcache = _batch.PlanCache(os.path.join(tempfile.mkdtemp(), "p.json"))
+        strategy, ttimes = _batch.autotune(tjobs, cache=tcache)
+        # the same tick with every frame on its tuned tile layout
+        tuned = _batch.tune_tiles(tjobs, cache=tcache)
+        tstrategy, tttimes = _batch.autotune(tuned, cache=tcache)
         tick_px = sum(j.outputs[0].shape[-1] * j.outputs[0].shape[-2] * len(j.outputs) for j in tjobs)
         configs["serving_tick_64_frames"] = {
             "frames": len(tjobs), "per_job_ms": per_job_ms, "batch_graph_ms": batch_ms,
             "batch_vs_per_job": per_job_ms / batch_ms, "autotuned": strategy, "times_ms": ttimes,
-            "out_mpix_s_batch": tick_px / (batch_ms / 1e3) / 1e6}
+            "out_mpix_s_batch": tick_px / (batch_ms / 1e3) / 1e6,
+            "tiles_tuned": {"autotuned": tstrategy, "times_ms": tttimes, "tile_layouts": _layouts(tuned)}}
+        del tuned
         del tjobs
         # NNEDI3 nns128-win8x6 on 4 frames of 1280x720, fast vs plain FP32
         nm = models["nnedi3-nns128-win8x6"]
@@ -708,6 +735,7 @@ def run_gpu(args, refs=None):
                           "how": "the same frames one launch chain after another on one stream; the roofline's "
                                  "per-launch kernel time comes from this loop"},
         "fp32_value": fp32_value, "chosen_vs_fp32": value / fp32_value,
+        "tile_sweep": tile_sweep,
         "e2e": {"value": e2e_value, "unit": "Mpix/s",
                 "h2d_bytes_per_step": int(host_in.numel() * host_in.element_size()),
                 "d2h_bytes_per_step": int(sum(t.numel() * t.element_size() for t in host_out.values()))},

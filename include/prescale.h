@@ -42,7 +42,7 @@
 extern "C" {
 #endif
 
-#define PZ_ABI_VERSION 1
+#define PZ_ABI_VERSION 2
 
 #define PZ_OK 0
 #define PZ_EINVAL (-22)
@@ -126,6 +126,13 @@ typedef struct {
   int staging;             /* RAVU halo staging: 0 clamped loads, 1 TMA boxes
                               for interior tiles (border tiles always use
                               clamped loads: TMA fills zeros, not the edge)  */
+  int tile_rows;           /* RAVU tile height: 4, 8 or 16 rows of 32 pixels
+                              (input pixels; ravu-zoom: output pixels), one
+                              thread per pixel; 0: the program's measured
+                              default (4 rows; ravu-lite r2 and ravu-lite-ar
+                              r4: 8).  The pixels do not depend on it.  The
+                              persistent batch kernels run 8-row tiles
+                              whatever this says.                           */
 } pz_opts;
 
 int pz_version(void);

@@ -62,7 +62,8 @@ class Plane(ctypes.Structure):
 class Opts(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("out_width", ctypes.c_int), ("out_height", ctypes.c_int),
                 ("nnedi3_axes", ctypes.c_int), ("keys", ctypes.c_void_p),
-                ("scratch", ctypes.c_void_p), ("scratch_bytes", ctypes.c_size_t), ("staging", ctypes.c_int)]
+                ("scratch", ctypes.c_void_p), ("scratch_bytes", ctypes.c_size_t), ("staging", ctypes.c_int),
+                ("tile_rows", ctypes.c_int)]
 
 
 class QueryResult(ctypes.Structure):

@@ -8,9 +8,11 @@ jobs run as their own passes.  ``Batch.capture()`` records the whole launch
 into a CUDA graph so that a steady-state batch costs one graph replay.
 
 ``autotune(jobs)`` times the execution strategies of a batch -- one launch
-per frame, or the persistent kernel with 1, 2 or as many CTAs per SM as fit
--- on the live device and caches the winner per GPU and batch signature in
-a JSON plan cache.
+per frame, each model's frames on its own side stream, or the persistent
+kernel with 1, 2 or as many CTAs per SM as fit -- on the live device and
+caches the winner per GPU and batch signature in a JSON plan cache;
+``autotune_tiles`` does the same for the tile layout of one model and frame
+shape (tile height x halo staging of the per-frame launches).
 """
 from __future__ import annotations
 
@@ -19,11 +21,11 @@ import hashlib
 import json
 import os
 import threading
-from dataclasses import dataclass, field
+from dataclasses import dataclass, field, replace
 from typing import Dict, List, Optional, Sequence, Tuple
 
 from . import _ffi
-from .prescaler import PRECISIONS, STAGINGS, HookModel
+from .prescaler import PRECISIONS, STAGINGS, TILE_ROWS, HookModel, check_tile_rows
 
 
 def _torch():
@@ -51,10 +53,11 @@ class Job:
     precision: str = "fp32"
     scratch: Optional["torch.Tensor"] = None
     staging: str = "tma"   # RAVU halo staging of interior tiles: "tma" boxes or "ldg" clamped loads
+    tile_rows: Optional[int] = None   # RAVU tile height of per-frame launches (4, 8, 16; None: the default)
 
     @staticmethod
     def make(model: HookModel, frame, out_size=None, precision="fp32", out=None, staging=None,
-             scratch=None) -> "Job":
+             scratch=None, tile_rows=None) -> "Job":
         """A job for ``frame`` ([H][W] or [C][H][W] CUDA tensor); allocates
         the outputs unless ``out`` is given, and the scratch the chain needs
         (NNEDI3's row-doubled plane, the ravu lattice's int11 plane) unless
@@ -75,11 +78,18 @@ class Job:
         staging = staging or model.default_staging
         if staging not in STAGINGS:
             raise ValueError(f"staging {staging!r}: one of {sorted(STAGINGS)}")
-        return Job(model, pl, outs, (OW, OH), precision, scratch, staging)
+        check_tile_rows(tile_rows)
+        return Job(model, pl, outs, (OW, OH), precision, scratch, staging, tile_rows)
 
     def signature(self) -> Tuple:
         p = self.inputs[0]
-        return (self.model.name, p.shape[1], p.shape[0], self.out_size, str(p.dtype), self.precision, self.staging)
+        return (self.model.name, p.shape[1], p.shape[0], self.out_size, str(p.dtype), self.precision, self.staging,
+                self.tile_rows)
+
+    def shape_key(self) -> Tuple:
+        """What the tile layout is tuned for: model, frame shape, dtype, output size, precision."""
+        p = self.inputs[0]
+        return (self.model.name, len(self.inputs), p.shape[1], p.shape[0], str(p.dtype), self.out_size, self.precision)
 
     def to_c(self) -> _ffi.Job:
         torch = _torch()
@@ -92,6 +102,7 @@ class Job:
         j.n_planes = len(self.inputs)
         j.opts.precision = PRECISIONS[self.precision]
         j.opts.staging = STAGINGS[self.staging]
+        j.opts.tile_rows = check_tile_rows(self.tile_rows)
         j.opts.out_width, j.opts.out_height = self.out_size
         if self.model.family == "nnedi3":
             W, H = self.inputs[0].shape[1], self.inputs[0].shape[0]
@@ -272,6 +283,60 @@ def autotune_staging(model: HookModel, frame, out_size=None, precision: str = "f
     return best, times
 
 
+def tile_layouts(model: HookModel) -> List[Tuple[str, int]]:
+    """The (staging, tile_rows) layouts a model's per-frame launches can run:
+    every tile height with both stagings (ravu-zoom stages by clamped loads
+    only); NNEDI3 has a single layout."""
+    if model.family == "nnedi3":
+        return [(model.default_staging, 8)]
+    stagings = ("ldg",) if model.family == "zoom" else ("ldg", "tma")
+    return [(st, r) for r in TILE_ROWS for st in stagings]
+
+
+def autotune_tiles(model: HookModel, frame, out_size=None, precision: str = "fp32",
+                   cache: Optional[PlanCache] = None, reps: int = 5) -> Tuple[Tuple[str, int], Dict[str, float]]:
+    """Time every tile layout (tile height x halo staging, ``tile_layouts``)
+    of one model and frame shape on this GPU; returns the fastest
+    ``(staging, tile_rows)`` and the times by ``"staging/rows"``.  Cached per
+    (GPU, model, shape, dtype, output size, precision)."""
+    torch = _torch()
+    cache = cache or PlanCache()
+    pl = [frame] if frame.dim() == 2 else list(frame.unbind(0))
+    H, W = pl[0].shape
+    OW, OH = model.output_size(W, H, out_size)
+    gpu = torch.cuda.get_device_name(frame.device)
+    key = f"{gpu}:tiles:{model.name}:{tuple(frame.shape)}:{frame.dtype}:{(OW, OH)}:{precision}"
+    hit = cache.get(key)
+    if hit:
+        return (hit["staging"], hit["tile_rows"]), hit.get("times_ms", {})
+    outs = [torch.empty((OH, OW), dtype=frame.dtype, device=frame.device) for _ in pl]
+    need = scratch_bytes(model, W, H, len(pl), pl[0].element_size(), (OW, OH))
+    scratch = torch.empty(need, dtype=torch.uint8, device=frame.device) if need else None
+    times = {}
+    for st, r in tile_layouts(model):
+        times[f"{st}/{r}"] = _time_ms(lambda st=st, r=r: model.run_raw(pl, outs, (OW, OH), precision=precision,
+                                                                       scratch=scratch, staging=st, tile_rows=r), reps)
+    best = min(times, key=times.get)
+    st, r = best.split("/")
+    cache.put(key, {"staging": st, "tile_rows": int(r), "times_ms": times})
+    return (st, int(r)), times
+
+
+def tune_tiles(jobs: Sequence[Job], cache: Optional[PlanCache] = None, reps: int = 5) -> List[Job]:
+    """The jobs with each one's tile layout set to the fastest for its model
+    and frame shape (``autotune_tiles``, once per distinct shape)."""
+    best: Dict[Tuple, Tuple[str, int]] = {}
+    out = []
+    for j in jobs:
+        k = j.shape_key()
+        if k not in best:
+            frame = j.inputs[0] if len(j.inputs) == 1 else _torch().stack(j.inputs)
+            best[k] = autotune_tiles(j.model, frame, j.out_size, j.precision, cache, reps)[0]
+        st, r = best[k]
+        out.append(replace(j, staging=st, tile_rows=r))
+    return out
+
+
 def _time_ms(fn, reps: int) -> float:
     torch = _torch()
     fn()
@@ -312,12 +377,17 @@ def autotune(jobs: Sequence[Job], cache: Optional[PlanCache] = None, reps: int =
 
 
 class Executor:
-    """Runs a fixed batch with its tuned strategy, replaying a CUDA graph."""
+    """Runs a fixed batch with its tuned strategy, replaying a CUDA graph.
+
+    With ``tune`` the jobs first take the fastest tile layout of their model
+    and frame shape (``tune_tiles``, unless ``tiles`` is false: the jobs'
+    own layouts; the per-frame strategies run it, the persistent kernels
+    run 8-row tiles), then the fastest strategy."""
 
     def __init__(self, jobs: Sequence[Job], cache: Optional[PlanCache] = None, tune: bool = True,
-                 use_graph: bool = True):
+                 use_graph: bool = True, tiles: bool = True):
         torch = _torch()
-        self.jobs = list(jobs)
+        self.jobs = tune_tiles(jobs, cache) if tune and tiles else list(jobs)
         self.strategy = autotune(self.jobs, cache)[0] if tune else "batch:0"
         self.batch = None
         self.graph = None

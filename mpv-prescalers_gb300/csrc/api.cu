@@ -140,11 +140,13 @@ int* device_error_word() {
   return g_err_words[dev];
 }
 
-int check_precision(const pz_opts* o, int dtype) {
+int check_opts(const pz_opts* o, int dtype) {
   if (o && (o->precision < PZ_PREC_FP32 || o->precision > PZ_PREC_MPV))
     return set_error(PZ_EINVAL, "unknown precision %d", o->precision);
   if (o && o->precision == PZ_PREC_MPV && dtype != PZ_F16)
     return set_error(PZ_EINVAL, "the mpv form takes FP16 planes (the host's textures are rgba16f)");
+  if (o && o->tile_rows != 0 && o->tile_rows != 4 && o->tile_rows != 8 && o->tile_rows != 16)
+    return set_error(PZ_EINVAL, "tile_rows %d: 0 (default), 4, 8 or 16", o->tile_rows);
   return PZ_OK;
 }
 }  // namespace pz
@@ -416,7 +418,7 @@ int pz_run(const pz_model* m, const pz_plane* in, int n_in, pz_plane* out, int n
       return fail(PZ_EINVAL, "output planes differ in size");
   }
   const int W = in[0].width, H = in[0].height, dt = in[0].dtype;
-  if ((rc = pz::check_precision(o, dt))) return rc;
+  if ((rc = pz::check_opts(o, dt))) return rc;
   int* err = pz::device_error_word();
   if (!err) return fail(PZ_EIO, "device error word: cudaGetSymbolAddress failed");
   int OW = 2 * W, OH = 2 * H;
@@ -498,6 +500,7 @@ int pz_run(const pz_model* m, const pz_plane* in, int n_in, pz_plane* out, int n
     a.keys = o ? o->keys : nullptr;
     a.err = err;
     a.staging = o ? o->staging : 0;
+    a.tile_rows = o && o->tile_rows ? o->tile_rows : pz::default_tile_rows(m);
     a.kp = m->kp;
     bool own_i11 = false;
     if (m->family == PZ_RAVU) {  // the int11 plane between the two lattice launches

@@ -130,7 +130,8 @@ int build_tables(const pz_job* jobs, int n, std::vector<pz::DevJob>* table, pz_b
     d.prog = en.prog;
     const bool zoom = m->family == PZ_RAVU_ZOOM;
     const int tw = ((zoom ? a.OW : a.W) + pz::kTileW - 1) / pz::kTileW;
-    const int th = ((zoom ? a.OH : a.H) + pz::kTileH - 1) / pz::kTileH;
+    const int th = ((zoom ? a.OH : a.H) + pz::kBatchTileRows - 1) / pz::kBatchTileRows;
+    a.tile_rows = pz::kBatchTileRows;
     d.tiles_w = tw;
     d.first_tile = g.total_tiles;
     // interior tiles of jobs that ask for TMA staging come in as TMA boxes
@@ -169,7 +170,7 @@ int validate_job(const pz_job& j, int idx) {
       return pz::set_error(PZ_EINVAL, "job %d: planes differ in size", idx);
   }
   int rc;
-  if ((rc = pz::check_precision(&j.opts, j.in[0].dtype))) return rc;
+  if ((rc = pz::check_opts(&j.opts, j.in[0].dtype))) return rc;
   const int W = j.in[0].width, H = j.in[0].height, OW = j.out[0].width, OH = j.out[0].height;
   const size_t es = j.in[0].dtype == PZ_F32 ? 4 : 2;
   switch (m->family) {

@@ -25,6 +25,7 @@ struct RavuArgs {
   int32_t* keys;     // optional raw-key output
   int* err;          // device error word (kErr*)
   int staging;       // 0: clamped loads, 1: TMA boxes for interior tiles
+  int tile_rows;     // tile height of the per-frame launches: 4, 8 or 16 rows
   float lut_frac;    // zoom LUT bilinear fraction steps (0: exact FP32)
   const uint2* lut_h;  // fast form: the LUT as FP16 texels (4 halves each), or null
   int lut_h_pitch;     // texels per FP16 LUT row (lut_cols rounded up to even)

@@ -34,9 +34,9 @@ int set_error(int code, const char* fmt, ...);
 // pz_check_device_error reads and clears it.
 int* device_error_word();
 
-// pz_run's checks of opts->precision against the plane dtype (PZ_OK or
-// PZ_EINVAL with the message set).
-int check_precision(const pz_opts* o, int dtype);
+// pz_run's checks of the options: opts->precision against the plane dtype,
+// opts->tile_rows (PZ_OK or PZ_EINVAL with the message set).
+int check_opts(const pz_opts* o, int dtype);
 
 // Does the fast form read this model's LUT as FP16 texels?  The lite, 3x and
 // zoom programs gather a whole LUT row (or four bilinear texels per block)
@@ -64,6 +64,16 @@ inline void select_lut(const pz_model* m, int precision, RavuArgs* a) {
   // the host's int11 texture is rgba16f: the mpv form rounds int11 to FP16,
   // the other forms keep it FP32 between the two lattice launches
   a->i11_half = mpv ? 1 : 0;
+}
+
+// Tile height of a model's per-frame launches when the caller asks for none,
+// the fastest on GB300 at 480p-1080p (1080p, fast form: 4-row tiles are
+// 3-4 % faster than 8 for ravu-r3 / ravu-r4-yuv, 8 % for ravu-3x-r3, even
+// for ravu-zoom-ar-r2-rgb; ravu-lite-r2 and ravu-lite-ar-r4 are fastest at
+// 8; 16 rows is slower for every program).
+inline int default_tile_rows(const pz_model* m) {
+  if (m->family == PZ_RAVU_LITE && (m->radius == 2 || (m->radius == 4 && m->ar != 0.0f))) return 8;
+  return 4;
 }
 
 // Scratch of a ravu lattice chain: the int11 plane, FP32 [channels][H][W].

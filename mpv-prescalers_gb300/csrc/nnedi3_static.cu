@@ -85,7 +85,7 @@ extern "C" int pz_nnedi3_run_static(const pz_model* m, const pz_plane* in, pz_pl
   int rc;
   if ((rc = check(in, "in", false)) || (rc = check(out, "out", (ax & 2) != 0))) return rc;
   if (out->dtype != in->dtype) return pz::set_error(PZ_EINVAL, "in and out must share one dtype");
-  if ((rc = pz::check_precision(o, in->dtype))) return rc;
+  if ((rc = pz::check_opts(o, in->dtype))) return rc;
   const int W = in->width, H = in->height, dt = in->dtype;
   const size_t es = dt == PZ_F32 ? 4 : 2;
   const int OW = (ax & 2) ? 2 * W : W, OH = (ax & 1) ? 2 * H : H;

@@ -1,40 +1,9 @@
 // Per-model launches of the ravu-lite(-ar) and ravu-3x tile programs
-// (ravu_tiles.cuh): one 256-thread CTA per 32x8 block of input pixels.
-#include "ravu_tiles.cuh"
+// (ravu_tiles.cuh) by tile height, and their persistent batch kernels.
+#include "ravu_lite_rows.cuh"
 
 namespace pz {
 namespace {
-
-template <typename T, bool H16>
-int launch_lite_t(const RavuArgs& a, int radius, bool ar, cudaStream_t s) {
-  const int tw = (a.W + kTileW - 1) / kTileW, th = (a.H + kTileH - 1) / kTileH;
-#define PZ_LITE(R)                                                      \
-  return ar ? launch_tiles<LiteTile<R, true, T, H16>>(a, tw, th, s)     \
-            : launch_tiles<LiteTile<R, false, T, H16>>(a, tw, th, s)
-  switch (radius) {
-    case 2: PZ_LITE(2);
-    case 3: PZ_LITE(3);
-    case 4: PZ_LITE(4);
-  }
-#undef PZ_LITE
-  return -95;
-}
-
-template <typename T, bool H16>
-int launch_3x_t(const RavuArgs& a, int radius, int cm, cudaStream_t s) {
-  const int tw = (a.W + kTileW - 1) / kTileW, th = (a.H + kTileH - 1) / kTileH;
-#define PZ_3X(R)                                                                         \
-  return cm == kLuma  ? launch_tiles<ThreeXTile<R, kLuma, T, H16>>(a, tw, th, s)        \
-         : cm == kYuv ? launch_tiles<ThreeXTile<R, kYuv, T, H16>>(a, tw, th, s)         \
-                      : launch_tiles<ThreeXTile<R, kRgb, T, H16>>(a, tw, th, s)
-  switch (radius) {
-    case 2: PZ_3X(2);
-    case 3: PZ_3X(3);
-    case 4: PZ_3X(4);
-  }
-#undef PZ_3X
-  return -95;
-}
 
 template <typename T>
 PersistentOps lite_ops(int prog) {
@@ -65,17 +34,20 @@ PersistentOps persistent_ops_lite(int prog, int dtype) {
   return dtype == 0 ? lite_ops<float>(prog) : lite_ops<__half>(prog);
 }
 
-// a.lut_h set (fast form): the programs read FP16 LUT texels
 int launch_lite(const RavuArgs& a, int radius, bool ar, int dtype, cudaStream_t s) {
-  if (a.lut_h)
-    return dtype == 0 ? launch_lite_t<float, true>(a, radius, ar, s) : launch_lite_t<__half, true>(a, radius, ar, s);
-  return dtype == 0 ? launch_lite_t<float, false>(a, radius, ar, s) : launch_lite_t<__half, false>(a, radius, ar, s);
+  switch (a.tile_rows) {
+    case 4: return launch_lite_rows<4>(a, radius, ar, dtype, s);
+    case 16: return launch_lite_rows<16>(a, radius, ar, dtype, s);
+    default: return launch_lite_rows<8>(a, radius, ar, dtype, s);
+  }
 }
 
 int launch_3x(const RavuArgs& a, int radius, int cm, int dtype, cudaStream_t s) {
-  if (a.lut_h)
-    return dtype == 0 ? launch_3x_t<float, true>(a, radius, cm, s) : launch_3x_t<__half, true>(a, radius, cm, s);
-  return dtype == 0 ? launch_3x_t<float, false>(a, radius, cm, s) : launch_3x_t<__half, false>(a, radius, cm, s);
+  switch (a.tile_rows) {
+    case 4: return launch_3x_rows<4>(a, radius, cm, dtype, s);
+    case 16: return launch_3x_rows<16>(a, radius, cm, dtype, s);
+    default: return launch_3x_rows<8>(a, radius, cm, dtype, s);
+  }
 }
 
 }  // namespace pz

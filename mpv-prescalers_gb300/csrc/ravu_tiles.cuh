@@ -1,4 +1,4 @@
-// RAVU tile programs: one 256-thread CTA computes one tile of outputs.
+// RAVU tile programs: one CTA of 32 x TR threads computes one tile of outputs.
 //
 // Each program is a struct with the shared-memory bytes it needs and a
 // device `run(p, x0, y0, smem)` that stages the tile (plus its radius halo)
@@ -13,9 +13,11 @@
 //   LatticeTile ravu-r3.hook:148-437 (compute/ravu-r3.hook:155-430)
 //   ZoomTile    ravu-zoom-r2.hook:15-139, compute/ravu-zoom-ar-r2-rgb.hook:15-238
 //
-// Input tiles are 32 x 8 input pixels (zoom: 32 x 8 output pixels); thread
-// t handles column t % 32 of row t / 32.  Out-of-range reads replicate the
-// edge texel (the mpv texture border mode).
+// Input tiles are 32 x TR input pixels (zoom: output pixels), TR = 4, 8 or 16
+// rows (a template argument of every program; 8 is the reference's own
+// workgroup height, compute/ravu-lite-r3.hook:22); thread t handles column
+// t % 32 of row t / 32.  Out-of-range reads replicate the edge texel (the mpv
+// texture border mode).
 #pragma once
 #include <cstddef>
 #include <cstring>
@@ -25,26 +27,19 @@
 
 namespace pz {
 
-constexpr int kTileW = 32, kTileH = 8, kTileThreads = 256;
+// Tile width in pixels (one warp per tile row); persistent batches run tiles
+// of kBatchTileRows rows.
+constexpr int kTileW = 32, kBatchTileRows = 8;
 
 __host__ __device__ constexpr int cabs(int v) { return v < 0 ? -v : v; }
 
-// Stage a (TW x TH) clamp-to-edge tile of one plane at origin (x0, y0).
-template <int TW, int TH, typename T>
-__device__ __forceinline__ void stage_tile(float* tile, const T* in, int pitch, int W, int H, int x0, int y0) {
-  for (int i = threadIdx.x; i < TW * TH; i += kTileThreads) {
-    const int ty = i / TW, tx = i % TW;
-    const int gx = clampi(x0 + tx, 0, W - 1), gy = clampi(y0 + ty, 0, H - 1);
-    tile[i] = ldp(in + (size_t)gy * pitch + gx);
-  }
-}
-
 // Stage all planes of a frame; RGB also gets a Rec.709 luma tile (the key
 // input); luma and yuv take their key input from plane 0.
-template <int CM, int TW, int TH, typename T>
+// NT threads share the work.
+template <int CM, int TW, int TH, int NT, typename T>
 __device__ __forceinline__ void stage_planes(float* tile, float* ltile, const RavuArgs& p, int x0, int y0) {
   constexpr int C = CM == kLuma ? 1 : 3;
-  for (int i = threadIdx.x; i < TW * TH; i += kTileThreads) {
+  for (int i = threadIdx.x; i < TW * TH; i += NT) {
     const int ty = i / TW, tx = i % TW;
     const int gx = clampi(x0 + tx, 0, p.W - 1), gy = clampi(y0 + ty, 0, p.H - 1);
     float v[3] = {0.f, 0.f, 0.f};
@@ -93,7 +88,7 @@ __device__ __forceinline__ float lds_f(const __half* p) { return __half2float(*p
 // set, the tile abandoned and TMA off for the rest of the CTA).  The outcome
 // of the wait is made uniform across the CTA, so every thread takes the same
 // path through the tile's barriers.
-template <int CM, int TW, int TH, typename T>
+template <int CM, int TW, int TH, int NT, typename T>
 __device__ int stage_planes_tma(const RavuArgs& p, TmaCtx* t, int x0, int y0, float* tile, float* ltile) {
   constexpr int C = CM == kLuma ? 1 : 3;
   constexpr int BW = tma_box_w<TW>();
@@ -111,7 +106,7 @@ __device__ int stage_planes_tma(const RavuArgs& p, TmaCtx* t, int x0, int y0, fl
     return -1;
   }
   t->phase ^= 1u;
-  for (int i = threadIdx.x; i < TW * TH; i += kTileThreads) {
+  for (int i = threadIdx.x; i < TW * TH; i += NT) {
     const int ty = i / TW, tx = i % TW;
     float v[3] = {0.f, 0.f, 0.f};
 #pragma unroll
@@ -135,11 +130,11 @@ __device__ __forceinline__ void tma_drain(const TmaCtx* t) {
 
 // Stage the frame tile by TMA when possible, else by clamped loads.
 // Returns false only when a TMA wait timed out (the tile is abandoned).
-template <int CM, int TW, int TH, typename T>
+template <int CM, int TW, int TH, int NT, typename T>
 __device__ __forceinline__ bool stage_frame(const RavuArgs& p, TmaCtx* t, int x0, int y0, float* tile,
                                             float* ltile) {
-  const int r = stage_planes_tma<CM, TW, TH, T>(p, t, x0, y0, tile, ltile);
-  if (r == 0) stage_planes<CM, TW, TH, T>(tile, ltile, p, x0, y0);
+  const int r = stage_planes_tma<CM, TW, TH, NT, T>(p, t, x0, y0, tile, ltile);
+  if (r == 0) stage_planes<CM, TW, TH, NT, T>(tile, ltile, p, x0, y0);
   return r >= 0;
 }
 
@@ -184,10 +179,12 @@ __host__ __device__ constexpr bool lite_ar_col(int c) {
   return R == 2 || cabs(c / (2 * R - 1) - (R - 1)) + cabs(c % (2 * R - 1) - (R - 1)) <= 2;
 }
 
-template <int R, bool AR, typename T, bool H16 = false>
+template <int R, bool AR, typename T, bool H16 = false, int TR = 8>
 struct LiteTile {
   static constexpr int N = 2 * R - 1, S = N * N, HALO = R - 1;
-  static constexpr int TW = kTileW + N - 1, TH = kTileH + N - 1;
+  static constexpr int kRows = TR, kThreads = kTileW * TR;
+  static constexpr bool kOutputTiles = false;
+  static constexpr int TW = kTileW + N - 1, TH = TR + N - 1;
   // the value tile; the anti-ringing powers are formed per tap in registers
   // (ar_pow2): a shared table of each texel's four powers, formed once per
   // texel, measured 2-13 % slower (an extra barrier, 8 KB more shared memory
@@ -195,9 +192,9 @@ struct LiteTile {
   static constexpr size_t smem_bytes = (size_t)((TW * TH + 3) & ~3) * 4;
 
   static constexpr int kPlanes = 1;
-  // ravu-lite-ar-r4 fits 5 CTAs per SM at <= 48 registers (measured 2 %
-  // faster); the other radii lose more to spills than they gain
-  static constexpr int kMinBlocks = (R == 4 && AR) ? 5 : 0;
+  // ravu-lite-ar-r4 at <= 48 registers (5 CTAs of 8 rows per SM) measured
+  // 2 % faster; the other radii lose more to spills than they gain
+  static constexpr int kMaxRegs = (R == 4 && AR) ? 48 : 0;
   // ravu-lite-ar-r2 / -r3 measured 2-5 % slower with the packed structure
   // tensor (register allocation of the anti-ringing sums)
   static constexpr bool kPackedTensor = !(R <= 3 && AR);
@@ -205,7 +202,7 @@ struct LiteTile {
 
   __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, TmaCtx* tma = nullptr) {
     float* tile = smem;
-    if (!stage_frame<kLuma, TW, TH, T>(p, tma, x0 - HALO, y0 - HALO, tile, nullptr)) return;
+    if (!stage_frame<kLuma, TW, TH, kThreads, T>(p, tma, x0 - HALO, y0 - HALO, tile, nullptr)) return;
     __syncthreads();
     const int tx = threadIdx.x % kTileW, ty = threadIdx.x / kTileW;
     const int gx = x0 + tx, gy = y0 + ty;
@@ -299,20 +296,22 @@ struct LiteTile {
 };
 
 // --------------------------------------------------------------- ravu-3x --
-template <int R, int CM, typename T, bool H16 = false>
+template <int R, int CM, typename T, bool H16 = false, int TR = 8>
 struct ThreeXTile {
   static constexpr int N = 2 * R - 1, S = N * N, HALO = R - 1;
-  static constexpr int TW = kTileW + N - 1, TH = kTileH + N - 1;
+  static constexpr int kRows = TR, kThreads = kTileW * TR;
+  static constexpr bool kOutputTiles = false;
+  static constexpr int TW = kTileW + N - 1, TH = TR + N - 1;
   static constexpr int C = CM == kLuma ? 1 : 3;
   static constexpr size_t smem_bytes = (size_t)(C + (CM == kRgb ? 1 : 0)) * TW * TH * 4;
   static constexpr int kPlanes = C;
-  static constexpr int kMinBlocks = 0;  // no launch-bounds minimum
+  static constexpr int kMaxRegs = 0;  // the compiler's own allocation
   using Elem = T;
 
   __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, TmaCtx* tma = nullptr) {
     float* tile = smem;
     float* ltile = smem + C * TW * TH;
-    if (!stage_frame<CM, TW, TH, T>(p, tma, x0 - HALO, y0 - HALO, tile, ltile)) return;
+    if (!stage_frame<CM, TW, TH, kThreads, T>(p, tma, x0 - HALO, y0 - HALO, tile, ltile)) return;
     __syncthreads();
     const int tx = threadIdx.x % kTileW, ty = threadIdx.x / kTileW;
     const int gx = x0 + tx, gy = y0 + ty;
@@ -429,23 +428,25 @@ __device__ __forceinline__ void ravu_filter(const float4* L, const Val& val, flo
 // thread stores its pixel's int11 value into the compact FP32 int11 plane
 // (p.i11, [C][H][W]): one coalesced 4-byte store per channel.  The lattice
 // program below writes every output pixel.
-template <int R, int CM, typename T>
+template <int R, int CM, typename T, int TR = 8>
 struct Int11Tile {
   static constexpr int N = 2 * R, S = N * N, HALO = R - 1;
-  static constexpr int TW = kTileW + N - 1, TH = kTileH + N - 1;
+  static constexpr int kRows = TR, kThreads = kTileW * TR;
+  static constexpr bool kOutputTiles = false;
+  static constexpr int TW = kTileW + N - 1, TH = TR + N - 1;
   static constexpr int C = CM == kLuma ? 1 : 3;
   static constexpr size_t smem_bytes = (size_t)(C + (CM == kRgb ? 1 : 0)) * TW * TH * 4;
   static constexpr int kPlanes = C;
-  // register caps measured best on GB300: r3 6 CTAs per SM (40 registers;
-  // 8 CTAs at 32 spill the packed structure tensor), r4 5, r2 the
+  // register caps measured best on GB300: r3 40 registers (6 CTAs of 8 rows
+  // per SM; 32 registers spill the packed structure tensor), r4 48, r2 the
   // compiler's own allocation
-  static constexpr int kMinBlocks = R == 3 ? 6 : (R == 4 ? 5 : 0);
+  static constexpr int kMaxRegs = R == 3 ? 40 : (R == 4 ? 48 : 0);
   using Elem = T;
 
   __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, TmaCtx* tma = nullptr) {
     float* tile = smem;
     float* ltile = smem + C * TW * TH;
-    if (!stage_frame<CM, TW, TH, T>(p, tma, x0 - HALO, y0 - HALO, tile, ltile)) return;
+    if (!stage_frame<CM, TW, TH, kThreads, T>(p, tma, x0 - HALO, y0 - HALO, tile, ltile)) return;
     __syncthreads();
     const int tx = threadIdx.x % kTileW, ty = threadIdx.x / kTileW;
     const int gx = x0 + tx, gy = y0 + ty;
@@ -497,17 +498,19 @@ __host__ __device__ constexpr int lat_dy(int k, int L) {
 // its edge: the clamp-to-edge of the int11 texture) are staged; each thread
 // then holds all four samples of its output 2x2 block -- input (0,0), int10
 // (1,0), int01 (0,1), int11 (1,1) -- and writes them as two pixel-pair rows.
-template <int R, int CM, typename T>
+template <int R, int CM, typename T, int TR = 8>
 struct LatticeTile {
   static constexpr int N = 2 * R, S = N * N;
-  static constexpr int TW = kTileW + N - 1, TH = kTileH + N - 1;
+  static constexpr int kRows = TR, kThreads = kTileW * TR;
+  static constexpr bool kOutputTiles = false;
+  static constexpr int TW = kTileW + N - 1, TH = TR + N - 1;
   static constexpr int C = CM == kLuma ? 1 : 3;
   static constexpr int PL = C + (CM == kRgb ? 1 : 0);  // planes per tile set
   static constexpr size_t smem_bytes = (size_t)2 * PL * TW * TH * 4;
   static constexpr int kPlanes = C;
-  // register caps measured best on GB300: r3 5 CTAs per SM, r4 3, r2 the
-  // compiler's own allocation
-  static constexpr int kMinBlocks = R == 3 ? 5 : (R == 4 ? 3 : 0);
+  // register caps measured best on GB300: r3 48 registers (5 CTAs of 8 rows
+  // per SM), r4 80 (3), r2 the compiler's own allocation
+  static constexpr int kMaxRegs = R == 3 ? 48 : (R == 4 ? 80 : 0);
   using Elem = T;
 
   __device__ static void run(const RavuArgs& p, int x0, int y0, float* smem, TmaCtx* tma = nullptr) {
@@ -515,9 +518,9 @@ struct LatticeTile {
     float* lin = tin + C * TW * TH;
     float* t11 = smem + PL * TW * TH;       // int11, offsets -R .. R-1
     float* l11 = t11 + C * TW * TH;
-    if (!stage_frame<CM, TW, TH, T>(p, tma, x0 - (R - 1), y0 - (R - 1), tin, lin)) return;
+    if (!stage_frame<CM, TW, TH, kThreads, T>(p, tma, x0 - (R - 1), y0 - (R - 1), tin, lin)) return;
     const size_t plane = (size_t)p.W * p.H;
-    for (int i = threadIdx.x; i < TW * TH; i += kTileThreads) {
+    for (int i = threadIdx.x; i < TW * TH; i += kThreads) {
       const int ty = i / TW, tx = i % TW;
       const int cx = clampi(x0 - R + tx, 0, p.W - 1), cy = clampi(y0 - R + ty, 0, p.H - 1);
       float v[3] = {0.f, 0.f, 0.f};
@@ -611,33 +614,36 @@ __device__ __forceinline__ float comp4(const float4& v, int i) {
   return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
 }
 
-// One thread per OUTPUT pixel; the tile is 32 x 8 output pixels and stages the
-// input rectangle they touch (at most (32+N+1) x (8+N+1) when upscaling;
+// One thread per OUTPUT pixel; the tile is 32 x TR output pixels and stages the
+// input rectangle they touch (at most (32+N+1) x (TR+N+1) when upscaling;
 // its origin follows from the tile's source positions, as the compute
 // shader's rect, compute/ravu-zoom-ar-r2.hook:28-37), by clamped loads of
 // just that rectangle: a fixed-size TMA box of the largest rectangle
 // converts up to 1.6x more texels at 1.5x and measured slower.
-template <int R, int CM, bool AR, typename T, bool H16 = false>
+template <int R, int CM, bool AR, typename T, bool H16 = false, int TR = 8>
 struct ZoomTile {
   static constexpr int N = 2 * R, S = N * N, LO = R - 1;
-  static constexpr int RW = kTileW + N + 1, RH = kTileH + N + 1;
+  static constexpr int kRows = TR, kThreads = kTileW * TR;
+  static constexpr bool kOutputTiles = true;
+  static constexpr int RW = kTileW + N + 1, RH = TR + N + 1;
   static constexpr int C = CM == kLuma ? 1 : 3;
   static constexpr int NB = (S / 2 + 3) / 4;  // LUT texels per half window
   // input rectangle planes, then the source positions of the tile's 32
-  // columns and 8 rows
+  // columns and TR rows
   static constexpr size_t smem_bytes =
-      (size_t)(C + (CM == kRgb ? 1 : 0)) * RW * RH * 4 + (kTileW + kTileH) * sizeof(ZoomPos);
+      (size_t)(C + (CM == kRgb ? 1 : 0)) * RW * RH * 4 + (kTileW + TR) * sizeof(ZoomPos);
 
   static constexpr int kPlanes = 0;  // clamped loads only
-  static constexpr int kMinBlocks = 0;  // no launch-bounds minimum
+  static constexpr int kMaxRegs = 0;  // the compiler's own allocation
   using Elem = T;
 
   __device__ static void run(const RavuArgs& p, int X0, int Y0, float* smem, TmaCtx* = nullptr) {
     float* tile = smem;
     float* ltile = smem + C * RW * RH;
     ZoomPos* pos = reinterpret_cast<ZoomPos*>(smem + (C + (CM == kRgb ? 1 : 0)) * RW * RH);
-    const int X1 = min(X0 + kTileW - 1, p.OW - 1), Y1 = min(Y0 + kTileH - 1, p.OH - 1);
-    if (threadIdx.x < kTileW + kTileH) {  // one exact position per tile column / row
+    const int X1 = min(X0 + kTileW - 1, p.OW - 1), Y1 = min(Y0 + TR - 1, p.OH - 1);
+    static_assert(kThreads >= kTileW + TR, "one thread per tile column and row");
+    if (threadIdx.x < kTileW + TR) {  // one exact position per tile column / row
       const int t = threadIdx.x;
       pos[t] = t < kTileW ? zoom_pos(min(X0 + t, X1), p.W, p.OW) : zoom_pos(min(Y0 + t - kTileW, Y1), p.H, p.OH);
     }
@@ -648,7 +654,7 @@ struct ZoomTile {
       if (threadIdx.x == 0 && p.err) atomicCAS(p.err, 0, kErrTileOverflow);
       return;
     }
-    for (int i = threadIdx.x; i < rw * rh; i += kTileThreads) {
+    for (int i = threadIdx.x; i < rw * rh; i += kThreads) {
       const int ty = i / rw, tx = i % rw;
       const int gx = clampi(rx + tx, 0, p.W - 1), gy = clampi(ry + ty, 0, p.H - 1);
       float v[3] = {0.f, 0.f, 0.f};
@@ -736,40 +742,44 @@ __device__ __forceinline__ void tile_body(const RavuArgs& p, const TmaMaps& maps
     __syncthreads();
     TmaCtx ctx{maps.map, smem_u32(&mbar),
                reinterpret_cast<unsigned char*>(tile_smem) + ((Prog::smem_bytes + 127) & ~(size_t)127), 0u, 0};
-    Prog::run(p, blockIdx.x * kTileW, blockIdx.y * kTileH, smem, &ctx);
+    Prog::run(p, blockIdx.x * kTileW, blockIdx.y * Prog::kRows, smem, &ctx);
     tma_drain(&ctx);
   } else {
-    Prog::run(p, blockIdx.x * kTileW, blockIdx.y * kTileH, smem, nullptr);
+    Prog::run(p, blockIdx.x * kTileW, blockIdx.y * Prog::kRows, smem, nullptr);
   }
 }
 
-// Programs with kMinBlocks > 0 ask the compiler for that many resident CTAs
-// per SM (a register cap); the others keep the compiler's own allocation.
+// Programs with kMaxRegs > 0 run under that register cap (the same cap at
+// every tile height); the others keep the compiler's own allocation.
 template <class Prog, bool TMA>
-__global__ void __launch_bounds__(kTileThreads) tile_kernel(const __grid_constant__ RavuArgs p,
-                                                            const __grid_constant__ TmaMaps maps) {
+__global__ void __launch_bounds__(Prog::kThreads) tile_kernel(const __grid_constant__ RavuArgs p,
+                                                              const __grid_constant__ TmaMaps maps) {
   tile_body<Prog, TMA>(p, maps);
 }
 template <class Prog, bool TMA>
-__global__ void __launch_bounds__(kTileThreads, Prog::kMinBlocks) tile_kernel_mb(const __grid_constant__ RavuArgs p,
-                                                                               const __grid_constant__ TmaMaps maps) {
+__global__ void __maxnreg__(Prog::kMaxRegs) tile_kernel_mr(const __grid_constant__ RavuArgs p,
+                                                           const __grid_constant__ TmaMaps maps) {
   tile_body<Prog, TMA>(p, maps);
 }
 
 template <class Prog, bool TMA>
 void launch_tile_kernel(dim3 grid, size_t smem, cudaStream_t s, const RavuArgs& a, const TmaMaps& maps) {
-  if constexpr (Prog::kMinBlocks > 0)
-    tile_kernel_mb<Prog, TMA><<<grid, kTileThreads, smem, s>>>(a, maps);
+  if constexpr (Prog::kMaxRegs > 0)
+    tile_kernel_mr<Prog, TMA><<<grid, Prog::kThreads, smem, s>>>(a, maps);
   else
-    tile_kernel<Prog, TMA><<<grid, kTileThreads, smem, s>>>(a, maps);
+    tile_kernel<Prog, TMA><<<grid, Prog::kThreads, smem, s>>>(a, maps);
 }
 
 bool encode_plane_map(CUtensorMap* map, const void* base, int W, int H, int pitch, int dtype, int box_w,
                       int box_h);
 
+// One CTA per tile of the frame (of the output frame for output-tiled
+// programs), staged by TMA when the frame asks for it and its planes map.
 template <class Prog>
-int launch_tiles(const RavuArgs& a, int tiles_w, int tiles_h, cudaStream_t s) {
+int launch_tiles(const RavuArgs& a, cudaStream_t s) {
   static_assert(Prog::smem_bytes <= 48 * 1024, "tile program needs more than the default shared memory");
+  const int fw = Prog::kOutputTiles ? a.OW : a.W, fh = Prog::kOutputTiles ? a.OH : a.H;
+  const int tiles_w = (fw + kTileW - 1) / kTileW, tiles_h = (fh + Prog::kRows - 1) / Prog::kRows;
   TmaMaps maps;
   std::memset(&maps, 0, sizeof maps);
   if constexpr (Prog::kPlanes > 0) {
@@ -871,7 +881,7 @@ __device__ __forceinline__ void persistent_body(const DevJob* __restrict__ jobs,
       loaded = job;
       const int* src = reinterpret_cast<const int*>(&jobs[loaded].a);
       int* dst = reinterpret_cast<int*>(&s_args);
-      for (int i = threadIdx.x; i < (int)(sizeof(RavuArgs) / 4); i += kTileThreads) dst[i] = src[i];
+      for (int i = threadIdx.x; i < (int)(sizeof(RavuArgs) / 4); i += Prog::kThreads) dst[i] = src[i];
       ctx.map = jobs[loaded].has_maps ? jobs[loaded].maps.map : nullptr;
       __syncthreads();
     }
@@ -879,19 +889,19 @@ __device__ __forceinline__ void persistent_body(const DevJob* __restrict__ jobs,
     // No barrier after the tile: the next tile's staging and argument copy
     // come after the next claim barrier, which every thread reaches only
     // when done with this tile.
-    Prog::run(s_args, (t % tw) * kTileW, (t / tw) * kTileH, smem, Prog::kPlanes > 0 ? &ctx : nullptr);
+    Prog::run(s_args, (t % tw) * kTileW, (t / tw) * Prog::kRows, smem, Prog::kPlanes > 0 ? &ctx : nullptr);
   }
   tma_drain(&ctx);
 }
 
 template <class Prog>
-__global__ void __launch_bounds__(kTileThreads) persistent_kernel(const DevJob* __restrict__ jobs, int n_jobs,
-                                                                  int total, int* counter) {
+__global__ void __launch_bounds__(Prog::kThreads) persistent_kernel(const DevJob* __restrict__ jobs, int n_jobs,
+                                                                    int total, int* counter) {
   persistent_body<Prog>(jobs, n_jobs, total, counter);
 }
 template <class Prog>
-__global__ void __launch_bounds__(kTileThreads, Prog::kMinBlocks) persistent_kernel_mb(
-    const DevJob* __restrict__ jobs, int n_jobs, int total, int* counter) {
+__global__ void __maxnreg__(Prog::kMaxRegs) persistent_kernel_mr(const DevJob* __restrict__ jobs, int n_jobs,
+                                                                 int total, int* counter) {
   persistent_body<Prog>(jobs, n_jobs, total, counter);
 }
 
@@ -931,23 +941,24 @@ template <class Prog>
 PersistentOps persistent_ops() {
   constexpr size_t kSmem = persistent_smem<Prog>();
   static_assert(kSmem <= 48 * 1024, "persistent tile program needs more than the default shared memory");
-  if constexpr (Prog::kMinBlocks > 0) {
+  static_assert(Prog::kRows == kBatchTileRows, "persistent batches number tiles of kBatchTileRows rows");
+  if constexpr (Prog::kMaxRegs > 0) {
     return {[](const DevJob* j, int n, int total, int* c, int grid, cudaStream_t s) {
-              persistent_kernel_mb<Prog><<<grid, kTileThreads, kSmem, s>>>(j, n, total, c);
+              persistent_kernel_mr<Prog><<<grid, Prog::kThreads, kSmem, s>>>(j, n, total, c);
             },
             []() {
               int fit = 0;
-              cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, persistent_kernel_mb<Prog>, kTileThreads, kSmem);
+              cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, persistent_kernel_mr<Prog>, Prog::kThreads, kSmem);
               return fit;
             },
             persistent_encode<Prog>};
   } else {
     return {[](const DevJob* j, int n, int total, int* c, int grid, cudaStream_t s) {
-              persistent_kernel<Prog><<<grid, kTileThreads, kSmem, s>>>(j, n, total, c);
+              persistent_kernel<Prog><<<grid, Prog::kThreads, kSmem, s>>>(j, n, total, c);
             },
             []() {
               int fit = 0;
-              cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, persistent_kernel<Prog>, kTileThreads, kSmem);
+              cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, persistent_kernel<Prog>, Prog::kThreads, kSmem);
               return fit;
             },
             persistent_encode<Prog>};

@@ -39,6 +39,18 @@ _CHANNEL_CODE = {"luma": _ffi.PZ_LUMA, "yuv": _ffi.PZ_YUV, "rgb": _ffi.PZ_RGB}
 PRECISIONS = {"fp32": _ffi.PZ_PREC_FP32, "fast": _ffi.PZ_PREC_FAST, "mpv": _ffi.PZ_PREC_MPV}
 # RAVU halo staging: clamped loads, or TMA boxes for interior tiles
 STAGINGS = {"ldg": 0, "tma": 1}
+# RAVU tile heights (rows of 32 pixels, one thread per pixel); None: the
+# library's measured default for the model's program
+TILE_ROWS = (4, 8, 16)
+
+
+def check_tile_rows(tile_rows) -> int:
+    """The ``pz_opts.tile_rows`` value of ``tile_rows`` (None: 0, the library's default)."""
+    if tile_rows is None:
+        return 0
+    if tile_rows not in TILE_ROWS:
+        raise ValueError(f"tile_rows {tile_rows!r}: one of {TILE_ROWS}")
+    return int(tile_rows)
 
 
 def _torch():
@@ -257,7 +269,8 @@ class HookModel:
 
     # ---- execution ----------------------------------------------------
     def upscale(self, planes: PlaneLike, out_size: Optional[Tuple[int, int]] = None, precision: str = "fp32",
-                out=None, return_keys: bool = False, stream=None, staging: Optional[str] = None):
+                out=None, return_keys: bool = False, stream=None, staging: Optional[str] = None,
+                tile_rows: Optional[int] = None):
         """Run the hook chain on ``planes``.
 
         ``planes``: a CUDA tensor ``[H][W]`` (luma), ``[C][H][W]`` (C = 1
@@ -275,6 +288,10 @@ class HookModel:
         (clamped loads) or "tma" (TMA boxes for interior tiles), default
         ``default_staging``; the pixels are identical, only the speed
         differs (see ``batch.autotune_staging``).
+        ``tile_rows``: RAVU tile height, 4, 8 or 16 rows of 32 pixels (one
+        thread per pixel; default: the library's measured choice for the
+        model's program, 4 rows but for ravu-lite r2 and ravu-lite-ar r4);
+        again only the speed differs (see ``batch.autotune_tiles``).
         Returns the upscaled planes in the input's form (and the raw LUT
         keys as int32 when ``return_keys``).
         """
@@ -285,7 +302,7 @@ class HookModel:
             with torch.cuda.stream(stream):
                 outs = [self.upscale(f, out_size=out_size, precision=precision,
                                      out=None if out is None else out[i], return_keys=return_keys, stream=stream,
-                                     staging=staging)
+                                     staging=staging, tile_rows=tile_rows)
                         for i, f in enumerate(planes.unbind(0))]
                 if return_keys:
                     return torch.stack([o[0] for o in outs]), torch.stack([o[1] for o in outs])
@@ -322,7 +339,7 @@ class HookModel:
             if return_keys:
                 keys = torch.empty(self.key_shape(W, H, OW, OH), dtype=torch.int32, device=dev)
             self.run_raw(pl, res, out_size=(OW, OH), precision=precision, keys=keys, stream=stream,
-                         staging=staging)
+                         staging=staging, tile_rows=tile_rows)
             return self._pack(res, planes, as_list, keys, return_keys, full)
 
     def upscale_host(self, frames, out=None, out_size: Optional[Tuple[int, int]] = None, precision: str = "fp32",
@@ -415,7 +432,8 @@ class HookModel:
             return (1,)
         return (H, W)
 
-    def run_raw(self, pl, res, out_size, precision="fp32", keys=None, stream=None, scratch=None, staging=None):
+    def run_raw(self, pl, res, out_size, precision="fp32", keys=None, stream=None, scratch=None, staging=None,
+                tile_rows=None):
         """Low-level call of ``pz_run`` on prepared tensors (no allocation
         besides the optional NNEDI3 scratch inside the library)."""
         torch = _torch()
@@ -437,6 +455,7 @@ class HookModel:
             o.scratch = scratch.data_ptr()
             o.scratch_bytes = scratch.numel() * scratch.element_size()
         o.staging = STAGINGS[staging or self.default_staging]
+        o.tile_rows = check_tile_rows(tile_rows)
         s = stream if stream is not None else torch.cuda.current_stream(pl[0].device)
         h = self.device_handle(pl[0].device.index)
         _ffi.check(_ffi.lib().pz_run(h, pin, n, pout, n, _ffi.ctypes.byref(o), s.cuda_stream))

@@ -38,7 +38,7 @@ def test_every_declared_symbol_is_exported(lib):
 
 
 def test_version_and_error_without_device(lib):
-    assert lib.pz_version() == 1
+    assert lib.pz_version() == 2
     assert isinstance(lib.pz_last_error(), bytes)
 
 
@@ -48,11 +48,35 @@ def test_null_arguments_are_rejected_on_the_host(lib):
     assert lib.pz_run(None, None, 0, None, 0, None, None) == _ffi.PZ_EINVAL
 
 
-def test_struct_layouts_match_the_header(lib):
+# ctypes mirror -> (C struct, {ctypes field: C field} where the names differ)
+_STRUCTS = {"ModelDesc": ("pz_model_desc", {}), "Plane": ("pz_plane", {}), "Opts": ("pz_opts", {}),
+            "QueryResult": ("pz_query_result", {}), "Job": ("pz_job", {"inp": "in"})}
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """Every ctypes mirror has the header struct's size and field offsets
+    (a C program compiled against include/prescale.h prints them)."""
     import ctypes
-    # pz_plane: void* + 4 ints
-    assert ctypes.sizeof(_ffi.Plane) == 8 + 4 * 4
-    assert ctypes.sizeof(_ffi.Opts) >= 4 * 4 + 8 + 8 + 8
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines, want = [], []
+    for py, (cs, rename) in _STRUCTS.items():
+        cls = getattr(_ffi, py)
+        lines.append(f'printf("%zu\\n", sizeof({cs}));')
+        want.append(ctypes.sizeof(cls))
+        for f, *_ in cls._fields_:
+            lines.append(f'printf("%zu\\n", offsetof({cs}, {rename.get(f, f)}));')
+            want.append(getattr(cls, f).offset)
+    src = tmp_path / "layout.c"
+    src.write_text("#include <stdio.h>\n#include <stddef.h>\n#include \"prescale.h\"\nint main(void) {\n" +
+                   "\n".join(lines) + "\nreturn 0;\n}\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert got == want
 
 
 def test_resample_arguments_are_checked_on_the_host(lib):

@@ -153,6 +153,56 @@ def test_tma_staging_gives_identical_pixels(name, dtype):
     assert torch.equal(a, b)
 
 
+@pytest.mark.parametrize("name", ["ravu-lite-ar-r4", "ravu-lite-r2", "ravu-r3", "ravu-r4-rgb", "ravu-3x-r3-yuv",
+                                  "ravu-zoom-ar-r2-rgb"])
+@pytest.mark.parametrize("rows", [4, 8, 16])
+@pytest.mark.parametrize("prec,dtype", [("fast", torch.float16), ("fp32", torch.float32)], ids=["fast", "fp32"])
+def test_tile_heights_give_identical_pixels(name, rows, prec, dtype):
+    """4-, 8- and 16-row tiles (both stagings) give the pixels and keys of the
+    default layout; 102 input rows (zoom: 181 output rows) leave a ragged
+    last tile row at every height."""
+    hm, _ = synth.model_for(name)
+    x = torch.from_numpy(synth.frame(102, 216, 63, hm.channels)).to("cuda", dtype)
+    osz = (400, 181) if hm.family == "zoom" else None
+    want, wkeys = hm.upscale(x, out_size=osz, precision=prec, staging="ldg", return_keys=True)
+    for st in ("ldg", "tma"):
+        got, keys = hm.upscale(x, out_size=osz, precision=prec, staging=st, tile_rows=rows, return_keys=True)
+        assert torch.equal(got, want), st
+        assert torch.equal(keys, wkeys), st
+
+
+def test_tile_rows_are_checked_by_the_library():
+    import ctypes
+    from mpv_prescalers_gb300 import _ffi
+    from mpv_prescalers_gb300 import batch as B
+    hm, _ = synth.model_for("ravu-lite-ar-r3")
+    x = torch.rand((40, 64), device="cuda")
+    y = torch.empty((80, 128), device="cuda")
+    pin = (_ffi.Plane * 1)(_ffi.Plane(x.data_ptr(), 64, 40, 64, _ffi.PZ_F32))
+    pout = (_ffi.Plane * 1)(_ffi.Plane(y.data_ptr(), 128, 80, 128, _ffi.PZ_F32))
+    o = _ffi.Opts()
+    L = _ffi.lib()
+    for bad in (1, 2, 5, 12, 32, -8):
+        o.tile_rows = bad
+        assert L.pz_run(hm.device_handle(0), pin, 1, pout, 1, ctypes.byref(o), None) == _ffi.PZ_EINVAL
+        assert b"tile_rows" in L.pz_last_error()
+    assert B.Job.make(hm, x, tile_rows=16).to_c().opts.tile_rows == 16
+    assert B.Job.make(hm, x).to_c().opts.tile_rows == 0
+
+
+def test_tile_autotuner(tmp_path):
+    from mpv_prescalers_gb300 import batch as B
+    hm, _ = synth.model_for("ravu-r3")
+    x = torch.rand((270, 480), device="cuda", dtype=torch.float16)
+    cache = B.PlanCache(str(tmp_path / "p.json"))
+    (st, rows), times = B.autotune_tiles(hm, x, precision="fast", cache=cache, reps=2)
+    assert st in ("ldg", "tma") and rows in (4, 8, 16)
+    assert set(times) == {f"{s}/{r}" for s, r in B.tile_layouts(hm)}
+    assert B.autotune_tiles(hm, x, precision="fast", cache=cache)[0] == (st, rows)   # cached
+    jobs = B.tune_tiles([B.Job.make(hm, x, precision="fast")], cache=cache)
+    assert (jobs[0].staging, jobs[0].tile_rows) == (st, rows)
+
+
 def test_tma_staging_falls_back_for_unaligned_pitch():
     hm, _ = synth.model_for("ravu-lite-ar-r3")
     big = torch.from_numpy(synth.luma_plane(90, 203, 62)).cuda()   # pitch 203 floats: not 16-byte rows

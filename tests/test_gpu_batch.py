@@ -91,6 +91,8 @@ def test_autotuner_picks_and_caches(tmp_path):
     again, _ = B.autotune(jobs, B.PlanCache(str(tmp_path / "plans.json")), reps=2)
     assert again == best
     ex = B.Executor(jobs, cache=cache)
+    # the executor's jobs carry the tuned tile layouts (same tensors)
+    assert all(e.tile_rows in (4, 8, 16) and e.outputs[0] is j.outputs[0] for e, j in zip(ex.jobs, jobs))
     ex.run()
     torch.cuda.synchronize()
     want = _expected(jobs)
@@ -112,7 +114,7 @@ def test_co_scheduled_streams_match_per_frame_launches(use_graph, tmp_path):
     cache = B.PlanCache(str(tmp_path / "plans.json"))
     key = B.PlanCache.key(torch.cuda.get_device_name(0), jobs)
     cache.put(key, {"strategy": "streams", "times_ms": {}})
-    ex = B.Executor(jobs, cache=cache, use_graph=use_graph)
+    ex = B.Executor(jobs, cache=cache, use_graph=use_graph, tiles=False)
     assert ex.strategy == "streams" and (ex.graph is not None) == use_graph
     for _ in range(2):
         ex.run()

@@ -97,6 +97,29 @@ def test_job_staging_is_checked_and_keyed():
     assert B.PlanCache.key("GB300", [a]) != B.PlanCache.key("GB300", [b])
 
 
+def test_job_tile_rows_are_checked_keyed_and_passed():
+    hm, _ = synth.model_for("ravu-lite-ar-r3")
+    x = torch.zeros((1, 36, 52), dtype=torch.float16)
+    for bad in (0, 2, 12, 32, "8"):
+        with pytest.raises(ValueError):
+            B.Job.make(hm, x, tile_rows=bad)
+    a, b, c = B.Job.make(hm, x), B.Job.make(hm, x), B.Job.make(hm, x, tile_rows=16)
+    assert B.PlanCache.key("GB300", [a]) == B.PlanCache.key("GB300", [b])
+    assert B.PlanCache.key("GB300", [a]) != B.PlanCache.key("GB300", [c])
+    assert a.shape_key() == c.shape_key()
+    from mpv_prescalers_gb300.prescaler import check_tile_rows
+    assert [check_tile_rows(r) for r in (None, 4, 8, 16)] == [0, 4, 8, 16]   # the pz_opts.tile_rows values
+
+
+def test_tile_layouts_per_family():
+    lite, _ = synth.model_for("ravu-lite-ar-r3")
+    zoom, _ = synth.model_for("ravu-zoom-ar-r2")
+    nn, _ = synth.model_for("nnedi3-nns16-win8x4")
+    assert sorted(B.tile_layouts(lite)) == sorted((st, r) for st in ("ldg", "tma") for r in (4, 8, 16))
+    assert B.tile_layouts(zoom) == [("ldg", 4), ("ldg", 8), ("ldg", 16)]   # clamped loads only
+    assert len(B.tile_layouts(nn)) == 1
+
+
 # ----------------------------------------------- request sizing / admission --
 
 def test_request_bytes():
