@@ -285,12 +285,10 @@ def autotune_staging(model: HookModel, frame, out_size=None, precision: str = "f
 
 def tile_layouts(model: HookModel) -> List[Tuple[str, int]]:
     """The (staging, tile_rows) layouts a model's per-frame launches can run:
-    every tile height with both stagings (ravu-zoom stages by clamped loads
-    only); NNEDI3 has a single layout."""
+    every tile height with both stagings; NNEDI3 has a single layout."""
     if model.family == "nnedi3":
         return [(model.default_staging, 8)]
-    stagings = ("ldg",) if model.family == "zoom" else ("ldg", "tma")
-    return [(st, r) for r in TILE_ROWS for st in stagings]
+    return [(st, r) for r in TILE_ROWS for st in ("ldg", "tma")]
 
 
 def autotune_tiles(model: HookModel, frame, out_size=None, precision: str = "fp32",

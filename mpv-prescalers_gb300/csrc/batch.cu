@@ -138,7 +138,7 @@ int build_tables(const pz_job* jobs, int n, std::vector<pz::DevJob>* table, pz_b
     // (the maps live in the device table); a map the driver rejects leaves
     // the job on clamped loads
     a.staging = j.opts.staging;
-    d.has_maps = j.opts.staging == 1 && g.ops.encode && g.ops.encode(a, &d.maps) ? 1 : 0;
+    d.has_maps = j.opts.staging == 1 && g.ops.encode && g.ops.encode(&a, &d.maps) ? 1 : 0;
     g.total_tiles += tw * th;
     table->push_back(d);
     g.n_jobs++;

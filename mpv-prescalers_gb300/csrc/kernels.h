@@ -29,6 +29,7 @@ struct RavuArgs {
   float lut_frac;    // zoom LUT bilinear fraction steps (0: exact FP32)
   const uint2* lut_h;  // fast form: the LUT as FP16 texels (4 halves each), or null
   int lut_h_pitch;     // texels per FP16 LUT row (lut_cols rounded up to even)
+  int box_w, box_h;    // ravu-zoom TMA staging: the box of this launch's tensor maps (texels x rows)
   float* i11;          // ravu lattice: int11 plane, FP32 [C][H][W] (scratch)
   int i11_half;        // round int11 to FP16 before storing it (the mpv form)
   KeyParams kp;

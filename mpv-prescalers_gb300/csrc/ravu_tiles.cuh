@@ -83,22 +83,23 @@ __host__ __device__ constexpr uint32_t tma_plane_bytes() {
 __device__ __forceinline__ float lds_f(const float* p) { return *p; }
 __device__ __forceinline__ float lds_f(const __half* p) { return __half2float(*p); }
 
-// 1: staged by TMA; 0: not an interior tile, or no maps (use clamped
-// loads); -1: the copy did not complete within the wait bound (error word
-// set, the tile abandoned and TMA off for the rest of the CTA).  The outcome
-// of the wait is made uniform across the CTA, so every thread takes the same
-// path through the tile's barriers.
-template <int CM, int TW, int TH, int NT, typename T>
-__device__ int stage_planes_tma(const RavuArgs& p, TmaCtx* t, int x0, int y0, float* tile, float* ltile) {
+// Stage a w x h window whose first texel is column `off` of a bw x bh TMA
+// box at (bx, by) (bx a multiple of 8): thread 0 issues one box per plane
+// into the landing area (plane stride pb bytes), the CTA waits for it, and
+// the window is converted to the float tile (row pitch dp, plane stride
+// dps; RGB also the luma tile).  Returns 1, or -1 when the copy did not complete within
+// the wait bound (error word set, the tile abandoned and TMA off for the
+// rest of the CTA).  The outcome of the wait is made uniform across the
+// CTA, so every thread takes the same path through the tile's barriers.
+template <int CM, int NT, typename T>
+__device__ __forceinline__ int tma_stage_box(const RavuArgs& p, TmaCtx* t, int bx, int by, int bw, int bh,
+                                             uint32_t pb, int off, int w, int h, int dp, int dps, float* tile,
+                                             float* ltile) {
   constexpr int C = CM == kLuma ? 1 : 3;
-  constexpr int BW = tma_box_w<TW>();
-  constexpr uint32_t PB = tma_plane_bytes<TW, TH, T>();
-  if (!t || !t->map || t->dead || x0 < 0 || y0 < 0 || x0 + TW > p.W || y0 + TH > p.H) return 0;
-  const int bx = x0 & ~7, off = x0 - bx;
   if (threadIdx.x == 0) {
-    mbar_arrive_expect_tx(t->mbar, (uint32_t)C * BW * TH * sizeof(T));
+    mbar_arrive_expect_tx(t->mbar, (uint32_t)C * bw * bh * sizeof(T));
 #pragma unroll
-    for (int c = 0; c < C; c++) tma_load_2d(t->raw + c * PB, &t->map[c], bx, y0, t->mbar);
+    for (int c = 0; c < C; c++) tma_load_2d(t->raw + c * pb, &t->map[c], bx, by, t->mbar);
   }
   if (!__syncthreads_and(mbar_wait_bounded(t->mbar, t->phase))) {
     if (threadIdx.x == 0 && p.err) atomicCAS(p.err, 0, kErrWaitTimeout);
@@ -106,17 +107,27 @@ __device__ int stage_planes_tma(const RavuArgs& p, TmaCtx* t, int x0, int y0, fl
     return -1;
   }
   t->phase ^= 1u;
-  for (int i = threadIdx.x; i < TW * TH; i += NT) {
-    const int ty = i / TW, tx = i % TW;
+  for (int i = threadIdx.x; i < w * h; i += NT) {
+    const int ty = i / w, tx = i % w;
     float v[3] = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int c = 0; c < C; c++) {
-      v[c] = lds_f(reinterpret_cast<const T*>(t->raw + c * PB) + ty * BW + tx + off);
-      tile[c * TW * TH + i] = v[c];
+      v[c] = lds_f(reinterpret_cast<const T*>(t->raw + c * pb) + ty * bw + tx + off);
+      tile[c * dps + ty * dp + tx] = v[c];
     }
-    if (CM == kRgb) ltile[i] = rgb_luma(v[0], v[1], v[2]);
+    if (CM == kRgb) ltile[ty * dp + tx] = rgb_luma(v[0], v[1], v[2]);
   }
   return 1;
+}
+
+// The TW x TH frame tile at (x0, y0) by TMA: 1 staged; 0 not an interior
+// tile, or no maps (use clamped loads); -1 the wait timed out.
+template <int CM, int TW, int TH, int NT, typename T>
+__device__ int stage_planes_tma(const RavuArgs& p, TmaCtx* t, int x0, int y0, float* tile, float* ltile) {
+  if (!t || !t->map || t->dead || x0 < 0 || y0 < 0 || x0 + TW > p.W || y0 + TH > p.H) return 0;
+  const int bx = x0 & ~7;
+  return tma_stage_box<CM, NT, T>(p, t, bx, y0, tma_box_w<TW>(), TH, tma_plane_bytes<TW, TH, T>(), x0 - bx, TW, TH,
+                                  TW, TW * TH, tile, ltile);
 }
 
 // A CTA whose TMA wait timed out may still have that copy in flight into its
@@ -617,9 +628,10 @@ __device__ __forceinline__ float comp4(const float4& v, int i) {
 // One thread per OUTPUT pixel; the tile is 32 x TR output pixels and stages the
 // input rectangle they touch (at most (32+N+1) x (TR+N+1) when upscaling;
 // its origin follows from the tile's source positions, as the compute
-// shader's rect, compute/ravu-zoom-ar-r2.hook:28-37), by clamped loads of
-// just that rectangle: a fixed-size TMA box of the largest rectangle
-// converts up to 1.6x more texels at 1.5x and measured slower.
+// shader's rect, compute/ravu-zoom-ar-r2.hook:28-37): by clamped loads, or
+// (TMA staging, interior rectangles) from one TMA box per plane whose size
+// the host fits to the launch's scale factor (zoom_tma_box), converting just
+// the rectangle.
 template <int R, int CM, bool AR, typename T, bool H16 = false, int TR = 8>
 struct ZoomTile {
   static constexpr int N = 2 * R, S = N * N, LO = R - 1;
@@ -633,11 +645,13 @@ struct ZoomTile {
   static constexpr size_t smem_bytes =
       (size_t)(C + (CM == kRgb ? 1 : 0)) * RW * RH * 4 + (kTileW + TR) * sizeof(ZoomPos);
 
-  static constexpr int kPlanes = 0;  // clamped loads only
+  static constexpr int kPlanes = C;
   static constexpr int kMaxRegs = 0;  // the compiler's own allocation
+  // the largest TMA box: the largest rectangle plus up to 7 lead columns
+  static constexpr int kBoxMaxW = (RW + 7 + 7) & ~7, kBoxMaxH = RH;
   using Elem = T;
 
-  __device__ static void run(const RavuArgs& p, int X0, int Y0, float* smem, TmaCtx* = nullptr) {
+  __device__ static void run(const RavuArgs& p, int X0, int Y0, float* smem, TmaCtx* tma = nullptr) {
     float* tile = smem;
     float* ltile = smem + C * RW * RH;
     ZoomPos* pos = reinterpret_cast<ZoomPos*>(smem + (C + (CM == kRgb ? 1 : 0)) * RW * RH);
@@ -654,7 +668,16 @@ struct ZoomTile {
       if (threadIdx.x == 0 && p.err) atomicCAS(p.err, 0, kErrTileOverflow);
       return;
     }
-    for (int i = threadIdx.x; i < rw * rh; i += kThreads) {
+    // every operand of these tests is uniform across the CTA
+    int staged = 0;
+    if (tma && tma->map && !tma->dead && rx >= 0 && ry >= 0 && rx + rw <= p.W && ry + rh <= p.H &&
+        (rx & 7) + rw <= p.box_w && rh <= p.box_h) {
+      const uint32_t pb = ((uint32_t)p.box_w * p.box_h * sizeof(T) + 127u) & ~127u;
+      staged = tma_stage_box<CM, kThreads, T>(p, tma, rx & ~7, ry, p.box_w, p.box_h, pb, rx & 7, rw, rh, RW,
+                                              RW * RH, tile, ltile);
+      if (staged < 0) return;
+    }
+    for (int i = threadIdx.x; !staged && i < rw * rh; i += kThreads) {
       const int ty = i / rw, tx = i % rw;
       const int gx = clampi(rx + tx, 0, p.W - 1), gy = clampi(ry + ty, 0, p.H - 1);
       float v[3] = {0.f, 0.f, 0.f};
@@ -773,6 +796,54 @@ void launch_tile_kernel(dim3 grid, size_t smem, cudaStream_t s, const RavuArgs& 
 bool encode_plane_map(CUtensorMap* map, const void* base, int W, int H, int pitch, int dtype, int box_w,
                       int box_h);
 
+// TMA boxes of a program.  The frame-tile programs have one fixed box (the
+// tile and its halo plus up to 7 lead columns).  ravu-zoom's box holds the
+// largest input rectangle of the launch's scale factor: n consecutive output
+// columns span at most floor((n-1) W / OW) + 1 source steps, plus the 2R
+// window (rows likewise), capped at the program's largest box; a tile whose
+// rectangle does not fit stages by clamped loads.
+template <class Prog>
+constexpr int tma_box_max_w() {
+  if constexpr (Prog::kOutputTiles) return Prog::kBoxMaxW;
+  else return tma_box_w<Prog::TW>();
+}
+template <class Prog>
+constexpr int tma_box_max_h() {
+  if constexpr (Prog::kOutputTiles) return Prog::kBoxMaxH;
+  else return Prog::TH;
+}
+template <class Prog>
+void tma_box_of(const RavuArgs& a, int* bw, int* bh) {
+  if constexpr (Prog::kOutputTiles) {
+    const int w = (int)((long long)(kTileW - 1) * a.W / a.OW) + 1 + Prog::N;
+    const int h = (int)((long long)(Prog::kRows - 1) * a.H / a.OH) + 1 + Prog::N;
+    *bw = ((w + 7 + 7) & ~7) < Prog::kBoxMaxW ? ((w + 7 + 7) & ~7) : Prog::kBoxMaxW;
+    *bh = h < Prog::kBoxMaxH ? h : Prog::kBoxMaxH;
+  } else {
+    *bw = tma_box_max_w<Prog>();
+    *bh = tma_box_max_h<Prog>();
+  }
+}
+// Shared memory of the landing area: one largest box per plane.
+template <class Prog>
+constexpr size_t tma_landing_bytes() {
+  return (size_t)Prog::kPlanes *
+         (((size_t)tma_box_max_w<Prog>() * tma_box_max_h<Prog>() * sizeof(typename Prog::Elem) + 127) & ~(size_t)127);
+}
+// The maps of a's input planes for Prog's box (recorded in a->box_w / box_h);
+// false when a plane cannot be mapped (alignment, a box larger than the plane).
+template <class Prog>
+bool encode_tma(RavuArgs* a, TmaMaps* maps) {
+  int bw, bh;
+  tma_box_of<Prog>(*a, &bw, &bh);
+  const int dt = sizeof(typename Prog::Elem) == 4 ? 0 : 1;
+  for (int c = 0; c < Prog::kPlanes; c++)
+    if (!encode_plane_map(&maps->map[c], a->in[c], a->W, a->H, a->in_pitch[c], dt, bw, bh)) return false;
+  a->box_w = bw;
+  a->box_h = bh;
+  return true;
+}
+
 // One CTA per tile of the frame (of the output frame for output-tiled
 // programs), staged by TMA when the frame asks for it and its planes map.
 template <class Prog>
@@ -783,19 +854,12 @@ int launch_tiles(const RavuArgs& a, cudaStream_t s) {
   TmaMaps maps;
   std::memset(&maps, 0, sizeof maps);
   if constexpr (Prog::kPlanes > 0) {
-    if (a.staging == 1) {
-      constexpr int BW = tma_box_w<Prog::TW>(), BH = Prog::TH;
-      const int dt = sizeof(typename Prog::Elem) == 4 ? 0 : 1;
-      bool ok = true;
-      for (int c = 0; c < Prog::kPlanes && ok; c++)
-        ok = encode_plane_map(&maps.map[c], a.in[c], a.W, a.H, a.in_pitch[c], dt, BW, BH);
-      if (ok) {
-        constexpr size_t smem = ((Prog::smem_bytes + 127) & ~(size_t)127) +
-                                (size_t)Prog::kPlanes * tma_plane_bytes<Prog::TW, Prog::TH, typename Prog::Elem>();
-        static_assert(smem <= 48 * 1024, "TMA staging needs more than the default shared memory");
-        launch_tile_kernel<Prog, true>(dim3(tiles_w, tiles_h), smem, s, a, maps);
-        return 0;
-      }
+    RavuArgs b = a;
+    if (a.staging == 1 && encode_tma<Prog>(&b, &maps)) {
+      constexpr size_t smem = ((Prog::smem_bytes + 127) & ~(size_t)127) + tma_landing_bytes<Prog>();
+      static_assert(smem <= 48 * 1024, "TMA staging needs more than the default shared memory");
+      launch_tile_kernel<Prog, true>(dim3(tiles_w, tiles_h), smem, s, b, maps);
+      return 0;
     }
   }
   launch_tile_kernel<Prog, false>(dim3(tiles_w, tiles_h), Prog::smem_bytes, s, a, maps);
@@ -909,8 +973,8 @@ __global__ void __maxnreg__(Prog::kMaxRegs) persistent_kernel_mr(const DevJob* _
 // kernel.
 struct PersistentOps {
   void (*launch)(const DevJob* jobs, int n_jobs, int total, int* counter, int grid, cudaStream_t s);
-  int (*fit)();                                     // resident CTAs per SM
-  bool (*encode)(const RavuArgs& a, TmaMaps* maps);  // false: the program stages by clamped loads
+  int (*fit)();                                // resident CTAs per SM
+  bool (*encode)(RavuArgs* a, TmaMaps* maps);  // false: the job stages by clamped loads
 };
 
 // Shared memory of a persistent CTA: the program's, then (programs with
@@ -918,23 +982,15 @@ struct PersistentOps {
 template <class Prog>
 constexpr size_t persistent_smem() {
   if constexpr (Prog::kPlanes > 0)
-    return ((Prog::smem_bytes + 127) & ~(size_t)127) +
-           (size_t)Prog::kPlanes * tma_plane_bytes<Prog::TW, Prog::TH, typename Prog::Elem>();
+    return ((Prog::smem_bytes + 127) & ~(size_t)127) + tma_landing_bytes<Prog>();
   else
     return Prog::smem_bytes;
 }
 
 template <class Prog>
-bool persistent_encode(const RavuArgs& a, TmaMaps* maps) {
-  if constexpr (Prog::kPlanes > 0) {
-    constexpr int BW = tma_box_w<Prog::TW>(), BH = Prog::TH;
-    const int dt = sizeof(typename Prog::Elem) == 4 ? 0 : 1;
-    for (int c = 0; c < Prog::kPlanes; c++)
-      if (!encode_plane_map(&maps->map[c], a.in[c], a.W, a.H, a.in_pitch[c], dt, BW, BH)) return false;
-    return true;
-  } else {
-    return false;
-  }
+bool persistent_encode(RavuArgs* a, TmaMaps* maps) {
+  if constexpr (Prog::kPlanes > 0) return encode_tma<Prog>(a, maps);
+  else return false;
 }
 
 template <class Prog>

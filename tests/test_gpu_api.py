@@ -144,7 +144,7 @@ def test_when_false_leaves_planes_untouched():
 @pytest.mark.parametrize("dtype", [torch.float32, torch.float16])
 def test_tma_staging_gives_identical_pixels(name, dtype):
     """Interior tiles staged by TMA boxes, border tiles by clamped loads: the
-    same pixels as clamped loads everywhere (zoom always uses clamped loads)."""
+    same pixels as clamped loads everywhere."""
     hm, _ = synth.model_for(name)
     x = torch.from_numpy(synth.frame(100, 216, 61, hm.channels)).to("cuda", dtype)
     osz = (400, 180) if hm.family == "zoom" else None
@@ -201,6 +201,29 @@ def test_tile_autotuner(tmp_path):
     assert B.autotune_tiles(hm, x, precision="fast", cache=cache)[0] == (st, rows)   # cached
     jobs = B.tune_tiles([B.Job.make(hm, x, precision="fast")], cache=cache)
     assert (jobs[0].staging, jobs[0].tile_rows) == (st, rows)
+
+
+@pytest.mark.parametrize("name", ["ravu-zoom-r2", "ravu-zoom-ar-r2-rgb", "ravu-zoom-r3-yuv", "ravu-zoom-ar-r3"])
+@pytest.mark.parametrize("osz", [(218, 101), (241, 131), (324, 150), (500, 101), (801, 367), (218, 370)],
+                         ids=["1.0x", "1.1x", "1.5x", "2.3x1x", "3.7x", "1x3.7x"])
+@pytest.mark.parametrize("prec,dtype", [("fast", torch.float16), ("fp32", torch.float32)], ids=["fast", "fp32"])
+def test_zoom_tma_rectangles_give_identical_pixels(name, osz, prec, dtype):
+    """ravu-zoom's input rectangles staged from TMA boxes fitted to the scale
+    factor (interior rectangles; the others by clamped loads) give the
+    clamped-load pixels at every scale, per axis, at every tile height."""
+    hm, _ = synth.model_for(name)
+    x = torch.from_numpy(synth.frame(100, 217, 64, hm.channels)).to("cuda", dtype)
+    assert hm.enabled(217, 100, osz)
+    want = hm.upscale(x, out_size=osz, precision=prec, staging="ldg")
+    for rows in (4, 8, 16):
+        assert torch.equal(hm.upscale(x, out_size=osz, precision=prec, staging="tma", tile_rows=rows), want), rows
+
+
+def test_zoom_tma_box_larger_than_the_plane_falls_back():
+    hm, _ = synth.model_for("ravu-zoom-ar-r2")
+    x = torch.rand((6, 20), device="cuda", dtype=torch.float16)   # smaller than any box
+    assert hm.enabled(20, 6, (37, 11))
+    assert torch.equal(hm.upscale(x, out_size=(37, 11), staging="tma"), hm.upscale(x, out_size=(37, 11), staging="ldg"))
 
 
 def test_tma_staging_falls_back_for_unaligned_pitch():

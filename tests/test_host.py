@@ -116,7 +116,7 @@ def test_tile_layouts_per_family():
     zoom, _ = synth.model_for("ravu-zoom-ar-r2")
     nn, _ = synth.model_for("nnedi3-nns16-win8x4")
     assert sorted(B.tile_layouts(lite)) == sorted((st, r) for st in ("ldg", "tma") for r in (4, 8, 16))
-    assert B.tile_layouts(zoom) == [("ldg", 4), ("ldg", 8), ("ldg", 16)]   # clamped loads only
+    assert sorted(B.tile_layouts(zoom)) == sorted(B.tile_layouts(lite))
     assert len(B.tile_layouts(nn)) == 1
 
 
