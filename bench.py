@@ -493,8 +493,10 @@ def run_gpu(args, refs=None):
 
     def e2e_step():
         # public API on host frames: H2D copy, upscale and D2H copy of frame i
-        # overlap with its neighbours on three streams; both models' calls are
-        # queued before waiting, and the step ends when every frame is back
+        # overlap with its neighbours (copy streams and the model's own side
+        # stream); both models' calls are queued before waiting, so their
+        # kernels share the GPU and their copies the host link, and the step
+        # ends when every frame is back
         pending = [models[n].upscale_host(host_in, out=host_out[n], precision="fast", wait=False)[1]
                    for n in MODELS]
         for ev in pending:
@@ -737,7 +739,8 @@ def run_gpu(args, refs=None):
         "fp32_value": fp32_value, "chosen_vs_fp32": value / fp32_value,
         "tile_sweep": tile_sweep,
         "e2e": {"value": e2e_value, "unit": "Mpix/s",
-                "h2d_bytes_per_step": int(host_in.numel() * host_in.element_size()),
+                # each model's call copies the frames in
+                "h2d_bytes_per_step": int(len(MODELS) * host_in.numel() * host_in.element_size()),
                 "d2h_bytes_per_step": int(sum(t.numel() * t.element_size() for t in host_out.values()))},
         "roofline": {"bound": "fp32", "kernel": "LiteTile<4, AR, half, FP16 texels> (ravu-lite-ar-r4, fast form)",
                      "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s", "frac": achieved_tf / peak_tf,

@@ -191,8 +191,10 @@ int pz_run(const pz_model* model, const pz_plane* in, int n_in, pz_plane* out, i
 /* ---- frames in host memory --------------------------------------------
  * For hosts that decode in software and hold frames in host memory: runs
  * the chain over n_frames frames, copying frame i in, running it and copying
- * it back while its neighbours' transfers run under its kernels (two copy
- * streams owned by the library, three device slots in `work`).  Frames are
+ * it back while its neighbours' transfers run under its kernels (a pair of
+ * copy streams owned by the library, three device slots in `work`; calls on
+ * different cuda_streams take different pairs from a pool of four, so two
+ * models' calls in flight together share the host link frame by frame).  Frames are
  * planar and unpadded: frame f, plane c starts at element
  * (f * n_planes + c) * height * width of host_in; host_out likewise at the
  * output size pz_query reports.  Page-locked host memory is needed for the

@@ -8,8 +8,13 @@
 // caller's work buffer.  Events order each slot's reuse (its previous frame
 // must have left the device before the next one lands), so no call waits on
 // the host; the caller's stream completes after the last frame is back.
+// Calls on different caller streams take different copy-stream pairs (a
+// small pool per device), so the results of two models' calls in flight
+// together leave the device as each frame is done instead of one call's
+// after the other's.
 #include <cstring>
 #include <mutex>
+#include <unordered_map>
 
 #include "../../include/prescale.h"
 #include "model.h"
@@ -18,6 +23,7 @@ namespace {
 
 constexpr int kDepth = 3;        // device slots in flight (one per stream)
 constexpr int kMaxDevices = 64;
+constexpr int kPairs = 4;        // copy-stream pairs per device
 
 size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 size_t elem(int dtype) { return dtype == PZ_F32 ? 4 : 2; }
@@ -41,25 +47,39 @@ int layout(const pz_model* m, int w, int h, int dtype, const pz_opts* o, Layout*
   return PZ_OK;
 }
 
-// Two copy streams per device, created on first use and kept for the
-// process (non-blocking: they never wait on the legacy default stream).
+// kPairs pairs of copy streams per device, created on first use and kept
+// for the process (non-blocking: they never wait on the legacy default
+// stream).  A caller stream keeps the pair it was first given (pairs are
+// handed out in turn), so its calls stay ordered on one pair.
 std::mutex g_stream_mu;
-cudaStream_t g_copy[kMaxDevices][2];
+cudaStream_t g_copy[kMaxDevices][kPairs][2];
+std::unordered_map<cudaStream_t, int> g_pair_of[kMaxDevices];
+int g_next_pair[kMaxDevices];
 
-int copy_streams(cudaStream_t* in, cudaStream_t* out) {
+int copy_streams(cudaStream_t caller, cudaStream_t* in, cudaStream_t* out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return pz::set_error(PZ_EIO, "cudaGetDevice: %s", cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return pz::set_error(PZ_ENOTSUP, "device %d beyond %d", dev, kMaxDevices);
   std::lock_guard<std::mutex> lk(g_stream_mu);
+  auto& pairs = g_pair_of[dev];
+  auto it = pairs.find(caller);
+  int p;
+  if (it != pairs.end()) {
+    p = it->second;
+  } else {
+    if (pairs.size() >= 1024) pairs.clear();  // forget streams long gone (a pairing, not a resource)
+    p = g_next_pair[dev]++ % kPairs;
+    pairs.emplace(caller, p);
+  }
   for (int k = 0; k < 2; k++) {
-    if (!g_copy[dev][k]) {
-      e = cudaStreamCreateWithFlags(&g_copy[dev][k], cudaStreamNonBlocking);
+    if (!g_copy[dev][p][k]) {
+      e = cudaStreamCreateWithFlags(&g_copy[dev][p][k], cudaStreamNonBlocking);
       if (e != cudaSuccess) return pz::set_error(PZ_EIO, "cudaStreamCreate: %s", cudaGetErrorString(e));
     }
   }
-  *in = g_copy[dev][0];
-  *out = g_copy[dev][1];
+  *in = g_copy[dev][p][0];
+  *out = g_copy[dev][p][1];
   return PZ_OK;
 }
 
@@ -84,7 +104,7 @@ extern "C" int pz_run_host(const pz_model* m, const void* host_in, void* host_ou
                          kDepth * L.slot_bytes);
   if (reinterpret_cast<uintptr_t>(work) % 256) return pz::set_error(PZ_EINVAL, "work must be 256-byte aligned");
   cudaStream_t s = static_cast<cudaStream_t>(stream), s_in, s_out;
-  if ((rc = copy_streams(&s_in, &s_out))) return rc;
+  if ((rc = copy_streams(s, &s_in, &s_out))) return rc;
 
   cudaEvent_t start, fin, copied[kDepth], done[kDepth], drained[kDepth];
   cudaEvent_t* all[] = {&start, &fin};

@@ -72,6 +72,7 @@ class HookModel:
         # copies run on the library's copy streams, which the allocator does
         # not track)
         self._host_work: Dict[Tuple[int, int], List[Tuple["torch.cuda.Event", "torch.Tensor"]]] = {}
+        self._side: Dict[int, "torch.cuda.Stream"] = {}   # per device: the host pipeline's default stream
 
     # ---- metadata -----------------------------------------------------
     @property
@@ -351,7 +352,10 @@ class HookModel:
         should be pinned).  With ``wait=False`` it returns ``(out, event)``
         as soon as the work is queued: ``out`` is complete once ``event`` (a
         CUDA event on ``stream``) has completed, so calls for several models
-        can overlap on the device.
+        can overlap on the device.  Without ``stream`` the call runs on a
+        side stream of this model (ordered after the work queued so far on
+        the current stream): the kernels of two models' calls share the GPU
+        and their copies share the host link.
         """
         torch = _torch()
         if frames.dim() != 4 or frames.is_cuda:
@@ -384,7 +388,11 @@ class HookModel:
         L = _ffi.lib()
         h = self.device_handle(dev.index)
         with torch.cuda.device(dev):
-            s = stream if stream is not None else torch.cuda.current_stream(dev)
+            if stream is None:
+                s = self._side_stream(dev)
+                s.wait_stream(torch.cuda.current_stream(dev))
+            else:
+                s = stream
             nbytes = max(int(L.pz_run_host_work_bytes(h, W, H, dt, _ffi.ctypes.byref(o))), 256)
             work = self._take_host_work(dev, nbytes)   # idle: the copies may start at once
             try:
@@ -401,6 +409,15 @@ class HookModel:
             return out, fin
 
     _HOST_WORK_KEEP = 8   # idle buffers kept per (device, size)
+
+    def _side_stream(self, dev):
+        """This model's side stream on ``dev`` (created on first use)."""
+        torch = _torch()
+        with self._lock:
+            s = self._side.get(dev.index)
+            if s is None:
+                s = self._side[dev.index] = torch.cuda.Stream(dev)
+            return s
 
     def _take_host_work(self, dev, nbytes: int):
         torch = _torch()
