@@ -8,7 +8,7 @@ namespace {
 template <typename T>
 PersistentOps lattice_ops(int prog) {
 #define PZ_P(id, Tile, R, CM) \
-  case id: return persistent_ops<Tile<R, CM, T>>();
+  case id: return persistent_ops<Tile<R, CM, T, kBatchTileRows>>();
   switch (prog) {
     PZ_P(kInt110 + 0, Int11Tile, 2, kLuma) PZ_P(kInt110 + 1, Int11Tile, 2, kYuv) PZ_P(kInt110 + 2, Int11Tile, 2, kRgb)
     PZ_P(kInt110 + 3, Int11Tile, 3, kLuma) PZ_P(kInt110 + 4, Int11Tile, 3, kYuv) PZ_P(kInt110 + 5, Int11Tile, 3, kRgb)

@@ -8,9 +8,9 @@ namespace {
 template <typename T>
 PersistentOps lite_ops(int prog) {
 #define PZ_L(id, R, AR, H) \
-  case id: return persistent_ops<LiteTile<R, AR, T, H>>();
+  case id: return persistent_ops<LiteTile<R, AR, T, H, kBatchTileRows>>();
 #define PZ_X(id, R, CM, H) \
-  case id: return persistent_ops<ThreeXTile<R, CM, T, H>>();
+  case id: return persistent_ops<ThreeXTile<R, CM, T, H, kBatchTileRows>>();
   switch (prog) {
     PZ_L(kLite0 + 0, 2, false, false) PZ_L(kLite0 + 1, 2, true, false) PZ_L(kLite0 + 2, 3, false, false)
     PZ_L(kLite0 + 3, 3, true, false) PZ_L(kLite0 + 4, 4, false, false) PZ_L(kLite0 + 5, 4, true, false)

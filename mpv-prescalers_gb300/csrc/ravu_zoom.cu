@@ -8,7 +8,7 @@ namespace {
 template <typename T>
 PersistentOps zoom_ops(int prog) {
 #define PZ_Z(id, R, CM, AR, H) \
-  case id: return persistent_ops<ZoomTile<R, CM, AR, T, H>>();
+  case id: return persistent_ops<ZoomTile<R, CM, AR, T, H, kBatchTileRows>>();
   switch (prog) {
     PZ_Z(kZoom0 + 0, 2, kLuma, false, false) PZ_Z(kZoom0 + 1, 2, kLuma, true, false)
     PZ_Z(kZoom0 + 2, 2, kYuv, false, false) PZ_Z(kZoom0 + 3, 2, kYuv, true, false)
