@@ -820,6 +820,8 @@ CASES = {
     "ravu-r3-fast": ("ravu-r3", None, "fast"),
     "ravu-3x-r3-fast": ("ravu-3x-r3", None, "fast"),
     "ravu-zoom-ar-r2-rgb-fast": ("ravu-zoom-ar-r2-rgb", (2880, 1620), "fast"),
+    # the same through TMA-staged input rectangles (a tile layout the tuner may pick)
+    "ravu-zoom-ar-r2-rgb-fast-tma": ("ravu-zoom-ar-r2-rgb", (2880, 1620), "fast", {"staging": "tma"}),
     "nnedi3-nns128-win8x6-fast": ("nnedi3-nns128-win8x6", None, "fast"),
     "nnedi3-nns128-win8x6-fp32": ("nnedi3-nns128-win8x6", None, "fp32"),
     # not a model: the OFFSET correction of a 3840x2160 FP16 plane (pz_resample,
@@ -834,7 +836,8 @@ def run_case(name: str) -> None:
     import torch
     _pkg()
     from mpv_prescalers_gb300 import synth
-    model, out_size, prec = CASES[name]
+    model, out_size, prec = CASES[name][:3]
+    layout = CASES[name][3] if len(CASES[name]) > 3 else {}
     src = "n/a"
     if name == "resample-2160p":
         from mpv_prescalers_gb300 import frame as _frame
@@ -851,7 +854,7 @@ def run_case(name: str) -> None:
     else:
         hm, src = synth.model_for(model)
         x = torch.from_numpy(synth.frame(H, W, SEED0, hm.channels)).to("cuda", torch.float16)
-        call = lambda: hm.upscale(x, out_size=out_size, precision=prec)
+        call = lambda: hm.upscale(x, out_size=out_size, precision=prec, **layout)
     for _ in range(3):
         call()
     torch.cuda.synchronize()
