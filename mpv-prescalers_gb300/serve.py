@@ -262,9 +262,17 @@ def summarize(done: Sequence[Request], peak_bytes: int = 0) -> Dict[str, float]:
             "span_s": span, "peak_hbm_gb": peak_bytes / 1e9}
 
 
-def serial_baseline(models: Dict[str, HookModel], trace: Sequence[Request]) -> Dict[str, float]:
-    """The same trace, one request at a time, FP32 planes, no overlap: each
-    request starts when it has arrived and the previous one has finished."""
+def serial_baseline(models: Dict[str, HookModel], trace: Sequence[Request], real_time: bool = True,
+                    passes: int = 1, precision: str = "fp32") -> Dict[str, float]:
+    """The same trace, one request at a time, no overlap: each request starts
+    when it has arrived and the previous one has finished.  ``precision``
+    "fp32": the plain form on FP32 planes (the frames converted once, before
+    timing); otherwise that form on the trace's own FP16 frames.
+    ``real_time``: requests are taken up at their arrival on the wall clock,
+    as a server would (the default); else back to back, each start moved to
+    ``max(arrival, previous finish)`` on a virtual clock (no idle time on
+    the device).  With ``passes`` > 1 the trace runs that many times and the
+    last pass is reported (the earlier ones warm its host frames)."""
     torch = _torch()
     dev = torch.device("cuda", torch.cuda.current_device())
     clock = 0.0
@@ -273,10 +281,12 @@ def serial_baseline(models: Dict[str, HookModel], trace: Sequence[Request]) -> D
     fp32: Dict[int, "torch.Tensor"] = {}          # one pinned FP32 copy per distinct trace frame
 
     def as_fp32(f):
+        if precision != "fp32":
+            return f
         if id(f) not in fp32:
             fp32[id(f)] = _pinned(f.float())
         return fp32[id(f)]
-    reqs = [Request(r.rid, r.stream_id, r.model, as_fp32(r.frame), r.arrival, r.out_size, "fp32")
+    reqs = [Request(r.rid, r.stream_id, r.model, as_fp32(r.frame), r.arrival, r.out_size, precision)
             for r in sorted(trace, key=lambda q: q.arrival)]
     for q in reqs:
         m = models[q.model]
@@ -284,19 +294,25 @@ def serial_baseline(models: Dict[str, HookModel], trace: Sequence[Request]) -> D
         OW, OH = m.output_size(W, H, q.out_size)
         key = (C, OH, OW)
         if key not in host_out:
-            host_out[key] = _pinned(torch.empty(key, dtype=torch.float32))
-    for q in reqs:
-        start = max(clock, q.arrival)
+            host_out[key] = _pinned(torch.empty(key, dtype=q.frame.dtype))
+    for _ in range(passes):
+        done, clock = [], 0.0
         torch.cuda.synchronize(dev)
-        t = time.perf_counter()
-        xd = q.frame.to(dev, non_blocking=True)
-        y = models[q.model].upscale(xd, out_size=q.out_size, precision="fp32")
-        q.output = host_out[tuple(y.shape)]
-        q.output.copy_(y, non_blocking=True)
-        torch.cuda.synchronize(dev)
-        clock = start + (time.perf_counter() - t)
-        q.finish = clock
-        done.append(q)
+        t0 = time.perf_counter()
+        for q in reqs:
+            if real_time:
+                while time.perf_counter() - t0 < q.arrival:
+                    time.sleep(min(2e-4, max(0.0, q.arrival - (time.perf_counter() - t0))))
+            start = max(clock, q.arrival)
+            t = time.perf_counter()
+            xd = q.frame.to(dev, non_blocking=True)
+            y = models[q.model].upscale(xd, out_size=q.out_size, precision=precision)
+            q.output = host_out[tuple(y.shape)]
+            q.output.copy_(y, non_blocking=True)
+            torch.cuda.synchronize(dev)
+            clock = (time.perf_counter() - t0) if real_time else start + (time.perf_counter() - t)
+            q.finish = clock
+            done.append(q)
     return summarize(done)
 
 

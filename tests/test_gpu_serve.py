@@ -49,7 +49,12 @@ def test_hbm_budget_bounds_the_bytes_in_flight(models):
     assert srv.in_use == 0
 
 
-def test_serial_baseline_runs_the_same_trace(models):
+@pytest.mark.parametrize("real_time", [True, False], ids=["real_time", "back_to_back"])
+def test_serial_baseline_runs_the_same_trace(models, real_time):
     trace = serve.poisson_trace(models, 8, rate=500.0, streams=4, seed=13, resolutions=SMALL, frame_pool=1)
-    stats = serve.serial_baseline(models, trace)
-    assert stats["requests"] == 8 and stats["p99_ms"] > 0
+    stats = serve.serial_baseline(models, trace, real_time=real_time, passes=2)
+    assert stats["requests"] == 8 and stats["p50_ms"] > 0 and stats["p99_ms"] >= stats["p50_ms"]
+    if real_time:   # the wall clock covers at least the arrivals
+        assert stats["span_s"] >= max(r.arrival for r in trace) - min(r.arrival for r in trace)
+    fast = serve.serial_baseline(models, trace, real_time=real_time, precision="fast")
+    assert fast["requests"] == 8
