@@ -298,6 +298,9 @@ def autotune_tiles(model: HookModel, frame, out_size=None, precision: str = "fp3
     ``(staging, tile_rows)`` and the times by ``"staging/rows"``.  Cached per
     (GPU, model, shape, dtype, output size, precision)."""
     torch = _torch()
+    layouts = tile_layouts(model)
+    if len(layouts) == 1:   # nothing to choose (NNEDI3)
+        return layouts[0], {}
     cache = cache or PlanCache()
     pl = [frame] if frame.dim() == 2 else list(frame.unbind(0))
     H, W = pl[0].shape
@@ -311,7 +314,7 @@ def autotune_tiles(model: HookModel, frame, out_size=None, precision: str = "fp3
     need = scratch_bytes(model, W, H, len(pl), pl[0].element_size(), (OW, OH))
     scratch = torch.empty(need, dtype=torch.uint8, device=frame.device) if need else None
     times = {}
-    for st, r in tile_layouts(model):
+    for st, r in layouts:
         times[f"{st}/{r}"] = _time_ms(lambda st=st, r=r: model.run_raw(pl, outs, (OW, OH), precision=precision,
                                                                        scratch=scratch, staging=st, tile_rows=r), reps)
     best = min(times, key=times.get)
