@@ -616,7 +616,7 @@ def run_gpu(args, refs=None):
         ms = a.elapsed_time(b) / 3
         configs["zoom_rgb_1.5x_2.25x_plus_ravu_r4_yuv_16_frames_each"] = {
             "jobs": len(jobs), "ms": ms, "out_mpix_s": out_px / (ms / 1e3) / 1e6, "strategy": ex.strategy,
-            "tile_layouts": _layouts(ex.jobs), "form": "FP16 planes, fast form"}
+            "times_ms": ex.times, "tile_layouts": _layouts(ex.jobs), "form": "FP16 planes, fast form"}
         del ex, jobs
         # one tick of a 64-stream player: a frame of each stream through the
         # serving mix (resolutions 480p-2160p, ravu-lite-ar-r3 / ravu-r4-yuv /

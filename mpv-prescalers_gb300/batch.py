@@ -389,7 +389,8 @@ class Executor:
                  use_graph: bool = True, tiles: bool = True):
         torch = _torch()
         self.jobs = tune_tiles(jobs, cache) if tune and tiles else list(jobs)
-        self.strategy = autotune(self.jobs, cache)[0] if tune else "batch:0"
+        # the strategy and the time of every candidate (ms per run; empty untuned)
+        self.strategy, self.times = autotune(self.jobs, cache) if tune else ("batch:0", {})
         self.batch = None
         self.graph = None
         if self.strategy.startswith("batch:"):
