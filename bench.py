@@ -12,7 +12,7 @@ Reported (one JSON line on rank 0):
 
 * ``value``: output Mpix/s of the chosen form (FP16 planes, FP16 LUT texels,
   FP32 math), all ranks together, inputs resident in HBM, the two models
-  co-scheduled on two side streams (``batch.run_streams``);
+  co-scheduled on side streams (``batch.run_streams``: two per model);
   ``single_stream``: the same with one launch chain after another (the
   roofline's per-launch kernel time comes from that loop); ``fp32_value``:
   the plain FP32 form (FP32 planes), single stream, on the same workload.
@@ -465,9 +465,9 @@ def run_gpu(args, refs=None):
     fp32_value = job_value(out_px_step, args.steps, ms32, world)
     kern_ms = statistics.mean(a.elapsed_time(b) for a, b in kev)
 
-    # the same step with the two models co-scheduled: each model's frames on
-    # its own side stream, forked from and joined back to the timed stream
-    # (batch.run_streams), so the two programs share the SMs
+    # the same step with the two models co-scheduled: each model's frames
+    # dealt to two side streams of its own, forked from and joined back to
+    # the timed stream (batch.run_streams), so the two programs share the SMs
     from mpv_prescalers_gb300 import batch as _batch
     co_jobs = [_batch.Job.make(models[n], x16[f], out=outs16[n][f], precision="fast") for n in MODELS
                for f in range(NFRAMES)]
@@ -741,8 +741,8 @@ def run_gpu(args, refs=None):
                    "frames_per_model": NFRAMES, "weights": {n: sources[n] for n in MODELS},
                    "l2": "per-model working set 166 MB (33 MB in + 133 MB out) > 129 MB L2",
                    "parallelism": f"replicas x{world}"},
-        "execution": "chosen form, the two models co-scheduled: each model's 8 frames on its own side stream "
-                     "forked from and joined to the timed stream (batch.run_streams)",
+        "execution": "chosen form, the two models co-scheduled: each model's 8 frames dealt to two side streams "
+                     "of its own, forked from and joined to the timed stream (batch.run_streams)",
         "single_stream": {"value": value, "ms_per_step": ms16 / args.steps,
                           "how": "the same frames one launch chain after another on one stream; the roofline's "
                                  "per-launch kernel time comes from this loop"},

@@ -193,24 +193,39 @@ def _pool_stream(device, k: int):
     return _STREAM_POOL[key]
 
 
-def run_streams(jobs: Sequence[Job], stream=None, max_streams: int = 4):
-    """The co-scheduled strategy: the jobs of each model go on their own side
-    stream (forked from and joined back to `stream`), one pz_run chain per
-    job, so that the programs of different models run at the same time and
-    fill each other's idle issue slots (e.g. an issue-bound program beside a
-    shared-memory-bound one).  Capturable in a CUDA graph (fork and join are
+def stream_lanes(jobs: Sequence[Job], per_model: int = 2) -> List[List[Job]]:
+    """The launch chains of the co-scheduled strategy: each model's jobs dealt
+    in turn to `per_model` chains (one chain when any two of them share a
+    scratch buffer, which must then be used in order)."""
+    groups: Dict[str, List[Job]] = {}
+    for j in jobs:
+        groups.setdefault(j.model.name, []).append(j)
+    lanes = []
+    for _, g in sorted(groups.items()):
+        ptrs = [j.scratch.data_ptr() for j in g if j.scratch is not None]
+        k = max(1, min(per_model, len(g))) if len(set(ptrs)) == len(ptrs) else 1
+        lanes.extend(g[r::k] for r in range(k))
+    return lanes
+
+
+def run_streams(jobs: Sequence[Job], stream=None, max_streams: int = 8, per_model: int = 2):
+    """The co-scheduled strategy: the jobs of each model go on side streams
+    of their own (forked from and joined back to `stream`; `per_model`
+    streams per model, the model's jobs dealt to them in turn), one pz_run
+    chain per job, so that the programs of different models run at the same
+    time and fill each other's idle issue slots (e.g. an issue-bound program
+    beside a shared-memory-bound one), and the launch boundaries of one
+    model's frames overlap.  Capturable in a CUDA graph (fork and join are
     stream waits)."""
     torch = _torch()
     dev = jobs[0].inputs[0].device
     main = stream if stream is not None else torch.cuda.current_stream(dev)
-    groups: Dict[str, List[Job]] = {}
-    for j in jobs:
-        groups.setdefault(j.model.name, []).append(j)
-    side = [_pool_stream(dev, k) for k in range(min(max_streams, len(groups)))]
+    lanes = stream_lanes(jobs, per_model)
+    side = [_pool_stream(dev, k) for k in range(min(max_streams, len(lanes)))]
     for s in side:
         s.wait_stream(main)
-    for i, (_, g) in enumerate(sorted(groups.items())):
-        run_per_job(g, stream=side[i % len(side)])
+    for i, lane in enumerate(lanes):
+        run_per_job(lane, stream=side[i % len(side)])
     for s in side:
         main.wait_stream(s)
 

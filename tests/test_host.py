@@ -86,6 +86,21 @@ def test_job_make_shapes(name, shape, osz, want, scratch):
     assert j.out_size == (want[1], want[0])
 
 
+def test_stream_lanes_deal_each_models_jobs_unless_scratch_is_shared():
+    lite, _ = synth.model_for("ravu-lite-ar-r3")
+    ravu, _ = synth.model_for("ravu-r3")
+    x = torch.zeros((1, 24, 40), dtype=torch.float16)
+    jobs = [B.Job.make(m, x) for m in (lite, ravu) for _ in range(5)]
+    lanes = B.stream_lanes(jobs, per_model=2)
+    assert [len(l) for l in lanes] == [3, 2, 3, 2]          # per model, dealt in turn
+    assert {j.model.name for j in lanes[0] + lanes[1]} == {"ravu-lite-ar-r3"}
+    assert sorted(id(j) for l in lanes for j in l) == sorted(id(j) for j in jobs)
+    assert [len(l) for l in B.stream_lanes(jobs, per_model=1)] == [5, 5]
+    shared = torch.empty(B.scratch_bytes(ravu, 40, 24, 1, 2, (80, 48)), dtype=torch.uint8)
+    sj = [B.Job.make(ravu, x, scratch=shared) for _ in range(4)]   # one scratch: one chain, in order
+    assert [len(l) for l in B.stream_lanes(sj, per_model=2)] == [4]
+
+
 def test_job_staging_is_checked_and_keyed():
     hm, _ = synth.model_for("ravu-lite-ar-r3")
     x = torch.zeros((1, 36, 52), dtype=torch.float16)
