@@ -541,33 +541,43 @@ def run_gpu(args, refs=None):
             b.record(stream)
             torch.cuda.synchronize()
             res[prec] = 4 * H * W * reps / (a.elapsed_time(b) / 1e3) / 1e6
-        # the batched form: all 8 FP16 frames as one persistent launch (NNEDI3:
-        # its stream-ordered passes) captured in a CUDA graph and replayed
+        # the batched form: all 8 FP16 frames through the batch executor (tile
+        # layout and strategy tuned on this GPU, replayed from a CUDA graph
+        # unless one launch chain per frame wins),
+        # and as one persistent launch (NNEDI3: its stream-ordered passes)
+        # captured in a CUDA graph and replayed
+        import tempfile
         from mpv_prescalers_gb300 import batch as _batch
         bjobs = [_batch.Job.make(hm, x16[f], precision="fast") for f in range(NFRAMES)]
+        ex = _batch.Executor(bjobs, cache=_batch.PlanCache(os.path.join(tempfile.mkdtemp(), "h.json")))
         plan = _batch.Batch(bjobs)
         plan.launch()
         plan.capture()
-        for _ in range(3):
-            plan.replay()
-        torch.cuda.synchronize()
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
         reps = 5
-        a.record(stream)
-        for _ in range(reps):
-            plan.replay()
-        b.record(stream)
-        torch.cuda.synchronize()
-        res["batched"] = NFRAMES * 4 * H * W * reps / (a.elapsed_time(b) / 1e3) / 1e6
+        for key, run in (("batched", ex.run), ("persistent", plan.replay)):
+            for _ in range(3):
+                run()
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(reps):
+                run()
+            b.record(stream)
+            torch.cuda.synchronize()
+            res[key] = NFRAMES * 4 * H * W * reps / (a.elapsed_time(b) / 1e3) / 1e6
+        res["strategy"] = ex.strategy
         plan.close()
-        del bjobs
+        del bjobs, ex
         headline[n] = {"chosen_mpix_s": res["fast"], "fp32_mpix_s": res["fp32"],
                        "ratio": res["fast"] / res["fp32"], "chosen": "FP16 planes" + (
                            ", FP16 tensor-core neurons" if n.startswith("nnedi3") else
                            ", FP16 LUT texels, FP32 math"),
                        "batched_mpix_s": res["batched"], "batched_ratio": res["batched"] / res["fp32"],
-                       "batched": f"{NFRAMES} FP16 frames per persistent launch, CUDA graph replay"}
+                       "batched": f"{NFRAMES} FP16 frames through batch.Executor (tile layout and strategy tuned "
+                                  f"on this GPU: '{res['strategy']}'; graph replay for the batch and stream strategies)",
+                       "persistent_mpix_s": res["persistent"],
+                       "persistent": f"{NFRAMES} FP16 frames per persistent launch, CUDA graph replay"}
 
     # ---- tile layouts of the workload's programs: every tile height x halo
     # staging of one 1080p FP16 frame, fast form (batch.autotune_tiles)
