@@ -101,6 +101,31 @@ def test_stream_lanes_deal_each_models_jobs_unless_scratch_is_shared():
     assert [len(l) for l in B.stream_lanes(sj, per_model=2)] == [4]
 
 
+def test_zoom_tma_box_covers_every_tile_rectangle():
+    """The TMA box of a ravu-zoom launch (tma_box_of in csrc/ravu_tiles.cuh)
+    assumes that n consecutive output columns span at most
+    floor((n-1) W / OW) + 1 source steps of the exact source position
+    floor(((2X+1) W - OW) / (2 OW)); checked here for n = 32 columns and
+    4 / 8 / 16 rows over many scale factors."""
+    def pos(W, OW):
+        X = np.arange(OW, dtype=np.int64)
+        return ((2 * X + 1) * W - OW) // (2 * OW)
+    rng = np.random.default_rng(3)
+    cases = [(W, OW) for W in (7, 30, 217, 1280, 1920) for OW in (W + 1, int(W * 1.5), 2 * W, int(W * 2.25) + 1,
+                                                                   int(W * 3.7))]
+    cases += [(int(w), int(w * f)) for w, f in zip(rng.integers(2, 4000, 200), rng.uniform(1.001, 6.0, 200))]
+    for W, OW in cases:
+        if OW <= W:
+            continue
+        p = pos(W, OW)
+        for n in (32, 4, 8, 16):
+            if OW < n:   # the tile is clipped to the frame: a shorter span
+                continue
+            bound = (n - 1) * W // OW + 1
+            span = int((p[n - 1:] - p[:OW - n + 1]).max())
+            assert span <= bound, (W, OW, n, span, bound)
+
+
 def test_job_staging_is_checked_and_keyed():
     hm, _ = synth.model_for("ravu-lite-ar-r3")
     x = torch.zeros((1, 36, 52), dtype=torch.float16)
