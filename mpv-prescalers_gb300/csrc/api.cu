@@ -145,6 +145,8 @@ int check_opts(const pz_opts* o, int dtype) {
     return set_error(PZ_EINVAL, "unknown precision %d", o->precision);
   if (o && o->precision == PZ_PREC_MPV && dtype != PZ_F16)
     return set_error(PZ_EINVAL, "the mpv form takes FP16 planes (the host's textures are rgba16f)");
+  if (o && (o->staging < 0 || o->staging > 1))
+    return set_error(PZ_EINVAL, "staging %d: 0 (clamped loads) or 1 (TMA boxes)", o->staging);
   if (o && o->tile_rows != 0 && o->tile_rows != 4 && o->tile_rows != 8 && o->tile_rows != 16)
     return set_error(PZ_EINVAL, "tile_rows %d: 0 (default), 4, 8 or 16", o->tile_rows);
   return PZ_OK;

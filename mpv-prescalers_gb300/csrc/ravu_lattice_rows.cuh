@@ -11,10 +11,10 @@ namespace pz {
 
 template <typename T, int TR>
 int launch_lattice_t(const RavuArgs& a, int radius, int cm, cudaStream_t s) {
-#define PZ_LAT(R, CM)                                  \
-  do {                                                 \
-    launch_tiles<Int11Tile<R, CM, T, TR>>(a, s);       \
-    return launch_tiles<LatticeTile<R, CM, T, TR>>(a, s); \
+#define PZ_LAT(R, CM)                                                 \
+  do {                                                                \
+    if (const int rc = launch_tiles<Int11Tile<R, CM, T, TR>>(a, s)) return rc; \
+    return launch_tiles<LatticeTile<R, CM, T, TR>>(a, s);             \
   } while (0)
 #define PZ_LAT_CM(R)                   \
   if (cm == kLuma) PZ_LAT(R, kLuma);   \

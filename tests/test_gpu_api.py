@@ -186,6 +186,11 @@ def test_tile_rows_are_checked_by_the_library():
         o.tile_rows = bad
         assert L.pz_run(hm.device_handle(0), pin, 1, pout, 1, ctypes.byref(o), None) == _ffi.PZ_EINVAL
         assert b"tile_rows" in L.pz_last_error()
+    o.tile_rows = 0
+    for bad in (-1, 2, 7):
+        o.staging = bad
+        assert L.pz_run(hm.device_handle(0), pin, 1, pout, 1, ctypes.byref(o), None) == _ffi.PZ_EINVAL
+        assert b"staging" in L.pz_last_error()
     assert B.Job.make(hm, x, tile_rows=16).to_c().opts.tile_rows == 16
     assert B.Job.make(hm, x).to_c().opts.tile_rows == 0
 
