@@ -87,9 +87,9 @@ __device__ __forceinline__ float lds_f(const __half* p) { return __half2float(*p
 // box at (bx, by) (bx a multiple of 8): thread 0 issues one box per plane
 // into the landing area (plane stride pb bytes), the CTA waits for it, and
 // the window is converted to the float tile (row pitch dp, plane stride
-// dps; RGB also the luma tile).  Returns 1, or -1 when the copy did not complete within
-// the wait bound (error word set, the tile abandoned and TMA off for the
-// rest of the CTA).  The outcome of the wait is made uniform across the
+// dps; RGB also the luma tile).  Returns 1, or -1 when the copy did not
+// complete within the wait bound (error word set, the tile abandoned and TMA
+// off for the rest of the CTA).  The outcome of the wait is made uniform across the
 // CTA, so every thread takes the same path through the tile's barriers.
 template <int CM, int NT, typename T>
 __device__ __forceinline__ int tma_stage_box(const RavuArgs& p, TmaCtx* t, int bx, int by, int bw, int bh,
@@ -630,7 +630,7 @@ __device__ __forceinline__ float comp4(const float4& v, int i) {
 // its origin follows from the tile's source positions, as the compute
 // shader's rect, compute/ravu-zoom-ar-r2.hook:28-37): by clamped loads, or
 // (TMA staging, interior rectangles) from one TMA box per plane whose size
-// the host fits to the launch's scale factor (zoom_tma_box), converting just
+// the host fits to the launch's scale factor (tma_box_of), converting just
 // the rectangle.
 template <int R, int CM, bool AR, typename T, bool H16 = false, int TR = 8>
 struct ZoomTile {
