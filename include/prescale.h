@@ -200,8 +200,9 @@ int pz_run(const pz_model* model, const pz_plane* in, int n_in, pz_plane* out, i
  * output size pz_query reports.  Page-locked host memory is needed for the
  * copies to overlap.  Asynchronous: `cuda_stream` completes once the last
  * frame is in host_out.  work: device memory of pz_run_host_work_bytes()
- * bytes, 256-byte aligned, not used by anything else until the stream has
- * passed this call.  The copies first wait for the work already queued on
+ * bytes (three frame slots; a call of n < 3 frames needs n thirds of it),
+ * 256-byte aligned, not used by anything else until the stream has passed
+ * this call.  The copies first wait for the work already queued on
  * cuda_stream (which may still use `work`); with PZ_HOST_WORK_IDLE in flags
  * the caller vouches that `work` is idle, and the first frame's copy starts
  * at once, so calls for several models overlap.  Replaces a host's

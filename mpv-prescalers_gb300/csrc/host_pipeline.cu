@@ -99,9 +99,11 @@ extern "C" int pz_run_host(const pz_model* m, const void* host_in, void* host_ou
   Layout L;
   int rc = layout(m, width, height, dtype, o, &L);
   if (rc) return rc;
-  if (work_bytes < kDepth * L.slot_bytes)
-    return pz::set_error(PZ_EINVAL, "work of %zu bytes, %d frames in flight need %zu", work_bytes, kDepth,
-                         kDepth * L.slot_bytes);
+  // one device slot per frame in flight: fewer frames than slots need fewer
+  const int depth = n_frames < kDepth ? n_frames : kDepth;
+  if (work_bytes < depth * L.slot_bytes)
+    return pz::set_error(PZ_EINVAL, "work of %zu bytes, %d frames in flight need %zu", work_bytes, depth,
+                         depth * L.slot_bytes);
   if (reinterpret_cast<uintptr_t>(work) % 256) return pz::set_error(PZ_EINVAL, "work must be 256-byte aligned");
   cudaStream_t s = static_cast<cudaStream_t>(stream), s_in, s_out;
   if ((rc = copy_streams(s, &s_in, &s_out))) return rc;
@@ -154,11 +156,11 @@ extern "C" int pz_run_host(const pz_model* m, const void* host_in, void* host_ou
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s_out, start, 0);
   }
   for (int i = 0; i < n_frames && e == cudaSuccess && rc == PZ_OK; i++) {
-    const int b = i % kDepth;
+    const int b = i % depth;
     char* d_in = slots + b * L.slot_bytes;
     char* d_out = d_in + align256(L.in_bytes);
     char* d_scr = d_out + align256(L.out_bytes);
-    if (i >= kDepth) e = cudaStreamWaitEvent(s_in, drained[b], 0);  // slot b's last frame has left
+    if (i >= depth) e = cudaStreamWaitEvent(s_in, drained[b], 0);  // slot b's last frame has left
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(d_in, hin + (size_t)i * L.in_bytes, L.in_bytes, cudaMemcpyHostToDevice, s_in);
     if (e == cudaSuccess) e = cudaEventRecord(copied[b], s_in);

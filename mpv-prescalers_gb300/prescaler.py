@@ -73,6 +73,7 @@ class HookModel:
         # not track)
         self._host_work: Dict[Tuple[int, int], List[Tuple["torch.cuda.Event", "torch.Tensor"]]] = {}
         self._side: Dict[int, "torch.cuda.Stream"] = {}   # per device: the host pipeline's default stream
+        self._host_opts: Dict[Tuple, "_ffi.Opts"] = {}    # pz_opts of host pipelines, per frame geometry
 
     # ---- metadata -----------------------------------------------------
     @property
@@ -379,12 +380,7 @@ class HookModel:
         elif tuple(out.shape) != (N, C, OH, OW) or out.dtype != frames.dtype or not out.is_contiguous():
             raise ValueError(f"out must be a contiguous {frames.dtype} tensor of shape {(N, C, OH, OW)}")
         dt = _ffi.PZ_F32 if frames.dtype == torch.float32 else _ffi.PZ_F16
-        o = _ffi.Opts()
-        o.precision = PRECISIONS[precision]
-        o.out_width, o.out_height = OW, OH
-        if self.family == "nnedi3":
-            o.nnedi3_axes = self.nnedi3_axes(W, H, out_size)
-        o.staging = STAGINGS[self.default_staging]
+        o = self.host_opts(W, H, out_size, precision)
         L = _ffi.lib()
         h = self.device_handle(dev.index)
         with torch.cuda.device(dev):
@@ -409,6 +405,23 @@ class HookModel:
             return out, fin
 
     _HOST_WORK_KEEP = 8   # idle buffers kept per (device, size)
+
+    def host_opts(self, W: int, H: int, out_size=None, precision: str = "fp32") -> "_ffi.Opts":
+        """The ``pz_opts`` of a host pipeline call on W x H frames (made once
+        per geometry and form and kept; the library copies them per call)."""
+        key = (W, H, out_size, precision)
+        o = self._host_opts.get(key)
+        if o is None:
+            OW, OH = self.output_size(W, H, out_size)
+            o = _ffi.Opts()
+            o.precision = PRECISIONS[precision]
+            o.out_width, o.out_height = OW, OH
+            if self.family == "nnedi3":
+                o.nnedi3_axes = self.nnedi3_axes(W, H, out_size)
+            o.staging = STAGINGS[self.default_staging]
+            with self._lock:
+                o = self._host_opts.setdefault(key, o)
+        return o
 
     def _side_stream(self, dev):
         """This model's side stream on ``dev`` (created on first use)."""

@@ -9,24 +9,28 @@ frames a player's render loop would hand to the hook chain).  The server
   execution slot is free -- requests arriving while others run are admitted
   as soon as memory and slots free up;
 * runs each admitted request on its slot's CUDA stream (host->device copy,
-  the model's kernels, device->host copy), so the work of different
+  the model's kernels, device->host copy, queued by one call of the
+  library's host pipeline, ``pz_run_host``), so the work of different
   requests overlaps on the device; in ``mode="batch"`` the requests admitted
   together are launched as one persistent batch (``batch.Batch``);
 * records per-request latency from arrival to the moment the output is back
   in host memory (CUDA event time), and reports p50/p99, throughput and the
   peak device memory in use.
 
-``serial_baseline`` runs the same trace one request at a time in plain FP32
-planes with no overlap, the comparison point for the served numbers.
+``serial_baseline`` runs the same trace one request at a time with no
+overlap (plain FP32 planes, or the trace's own form), the comparison point
+for the served numbers.
 """
 from __future__ import annotations
 
+import ctypes
 import time
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
 
+from . import _ffi
 from . import batch as _batch
 from .prescaler import HookModel
 
@@ -172,6 +176,11 @@ class Server:
             # arena can go; the new one is allocated once for all later groups
             slot.arena = None
             slot.arena = torch.empty(need, dtype=torch.uint8, device=self.device)
+        if len(reqs) == 1:
+            self._launch_one(slot, reqs[0])
+            reqs[0].admit = now
+            slot.reqs = reqs
+            return
         off = 0
         with torch.cuda.stream(slot.stream):
             for r in reqs:
@@ -206,6 +215,28 @@ class Server:
         for r in reqs:
             r.admit = now
         slot.reqs = reqs
+
+    def _launch_one(self, slot: _Slot, r: Request):
+        """One request through the library's host pipeline (pz_run_host):
+        upload, kernels and readback are queued from native code, on the
+        slot's stream and a pair of copy streams, with the request's device
+        planes in the slot's arena (one frame slot of the pipeline)."""
+        torch = _torch()
+        m = self.models[r.model]
+        C, H, W = r.frame.shape
+        if r.frame.is_cuda or not r.frame.is_contiguous():
+            raise ValueError("request frames are contiguous host tensors [C][H][W]")
+        OW, OH = m.output_size(W, H, r.out_size)
+        if not (r.output is not None and tuple(r.output.shape) == (C, OH, OW) and r.output.dtype == r.frame.dtype
+                and r.output.is_contiguous() and r.output.is_pinned()):
+            r.output = torch.empty((C, OH, OW), dtype=r.frame.dtype, pin_memory=True)
+        dt = _ffi.PZ_F32 if r.frame.dtype == torch.float32 else _ffi.PZ_F16
+        o = m.host_opts(W, H, r.out_size, r.precision)
+        _ffi.check(_ffi.lib().pz_run_host(m.device_handle(self.device.index), r.frame.data_ptr(), r.output.data_ptr(),
+                                          1, W, H, dt, ctypes.byref(o), slot.arena.data_ptr(), slot.arena.numel(),
+                                          _ffi.PZ_HOST_WORK_IDLE, slot.stream.cuda_stream))
+        slot.done = torch.cuda.Event(enable_timing=True)
+        slot.done.record(slot.stream)
 
     def run(self, trace: Sequence[Request], max_group: int = 4) -> Dict[str, float]:
         """Serve a trace in real time; returns latency / throughput stats

@@ -99,14 +99,15 @@ def test_host_pipeline_c_abi_checks_work_and_layout():
     L = _ffi.lib()
     h = hm.device_handle(0)
     need = L.pz_run_host_work_bytes(h, 28, 20, _ffi.PZ_F16, ctypes.byref(o))
-    assert need >= 3 * (3 * 20 * 28 * 2 + 3 * 40 * 56 * 2)
+    assert need >= 3 * (3 * 20 * 28 * 2 + 3 * 40 * 56 * 2) and need % 3 == 0
     work = torch.empty(need, dtype=torch.uint8, device="cuda")
     s = torch.cuda.current_stream()
+    slot = need // 3   # one frame in flight: one of the three slots
     rc = L.pz_run_host(h, frames.data_ptr(), out.data_ptr(), 1, 28, 20, _ffi.PZ_F16, ctypes.byref(o),
-                       work.data_ptr(), need - 256, 0, s.cuda_stream)
+                       work.data_ptr(), slot - 256, 0, s.cuda_stream)
     assert rc == _ffi.PZ_EINVAL and b"work" in L.pz_last_error()
     _ffi.check(L.pz_run_host(h, frames.data_ptr(), out.data_ptr(), 1, 28, 20, _ffi.PZ_F16, ctypes.byref(o),
-                             work.data_ptr(), need, 0, s.cuda_stream))
+                             work.data_ptr(), slot, 0, s.cuda_stream))
     s.synchronize()
     assert torch.equal(out[0], hm.upscale(frames[0].cuda()).cpu())
     with pytest.raises(ValueError, match="contiguous"):
